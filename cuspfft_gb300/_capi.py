@@ -1,0 +1,116 @@
+"""ctypes binding of the C ABI declared in include/gbspfft.h.
+
+The shared library is built in-tree (cuspfft_gb300/_build/libgbspfft.so) by
+cuspfft_gb300.build; importing this module loads it and fails loudly when it
+is missing: there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libgbspfft.so"
+
+GBSP_OK = 0
+GBSP_ERR_INVALID = 1
+GBSP_ERR_CUDA = 2
+GBSP_ERR_ALLOC = 3
+GBSP_ERR_UNSUPPORTED = 4
+GBSP_ERR_IO = 5
+GBSP_ERR_NOT_BUILT = 6
+GBSP_LEN_3SMOOTH = 3
+GBSP_LEN_7SMOOTH = 7
+
+# Every symbol include/gbspfft.h declares; tests check the library exports them.
+EXPORTED = (
+    "gbsp_version", "gbsp_status_string", "gbsp_last_error", "gbsp_read_mtx", "gbsp_free",
+    "gbsp_build_compact_csc", "gbsp_next_smooth", "gbsp_plan_create", "gbsp_plan_get_info",
+    "gbsp_plan_destroy", "gbsp_execute", "gbsp_column_sums",
+)
+
+
+class GbspOptions(C.Structure):
+    _fields_ = [
+        ("length_policy", C.c_int),
+        ("u_tile", C.c_int),
+        ("kahan_min_degree", C.c_int),
+        ("index_bytes", C.c_int),
+        ("max_channel_len", C.c_int),
+        ("pass1_threads", C.c_int),
+        ("reserved", C.c_int * 8),
+    ]
+
+
+class GbspPlanInfo(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int), ("cols", C.c_int), ("nnz", C.c_int), ("n_active", C.c_int),
+        ("fft_len", C.c_int), ("channels", C.c_int), ("channel_len", C.c_int),
+        ("n_stages", C.c_int), ("radix", C.c_int * 16), ("output_cols", C.c_int),
+        ("output_pitch", C.c_int), ("half_rows", C.c_int), ("u_tile", C.c_int),
+        ("index_bytes", C.c_int), ("row_table_mode", C.c_int), ("device_bytes", C.c_size_t),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {name: getattr(self, name) for name, _ in self._fields_ if name != "radix"}
+        d["radix"] = [self.radix[i] for i in range(self.n_stages)]
+        return d
+
+
+class GbspError(RuntimeError):
+    def __init__(self, status: int, what: str, msg: str):
+        super().__init__(f"{what}: {status_string(status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Returns the loaded library, building it first if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists() and build_if_missing and os.environ.get("GBSP_NO_AUTOBUILD") != "1":
+        from . import build as _build
+        _build.build()
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"cuspfft_gb300 native library missing: {LIB_PATH} (run cuspfft_gb300.build)")
+    lib = C.CDLL(str(LIB_PATH))
+    vp, ip, i32 = C.c_void_p, C.POINTER(C.c_int), C.c_int
+    lib.gbsp_version.restype = i32
+    lib.gbsp_status_string.restype = C.c_char_p
+    lib.gbsp_status_string.argtypes = [i32]
+    lib.gbsp_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    lib.gbsp_read_mtx.argtypes = [C.c_char_p, ip, ip, ip, C.POINTER(ip), C.POINTER(ip)]
+    lib.gbsp_free.argtypes = [vp]
+    lib.gbsp_free.restype = None
+    lib.gbsp_build_compact_csc.argtypes = [i32, i32, i32, ip, ip, ip, ip, ip, ip]
+    lib.gbsp_next_smooth.argtypes = [i32, i32]
+    lib.gbsp_plan_create.argtypes = [i32, i32, i32, i32, ip, ip, ip, C.POINTER(GbspOptions), vp,
+                                     C.POINTER(vp)]
+    lib.gbsp_plan_get_info.argtypes = [vp, C.POINTER(GbspPlanInfo)]
+    lib.gbsp_plan_destroy.argtypes = [vp]
+    lib.gbsp_execute.argtypes = [vp, vp, C.c_size_t, vp]
+    lib.gbsp_column_sums.argtypes = [vp, i32, i32, vp, C.c_size_t, vp]
+    for name in EXPORTED:
+        if name not in ("gbsp_status_string", "gbsp_free"):
+            getattr(lib, name).restype = i32
+    _lib = lib
+    return lib
+
+
+def status_string(status: int) -> str:
+    return load().gbsp_status_string(status).decode()
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    load().gbsp_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int, what: str) -> None:
+    if status != GBSP_OK:
+        raise GbspError(status, what, last_error())

@@ -1,0 +1,459 @@
+// gbsp_plan.cu -- plans and execution behind the C ABI (include/gbspfft.h).
+//
+// A plan owns everything the timed loop reads: the uploaded compact CSC, the
+// FP64-built tables rounded to FP32, and the pass-1 scratch tile.  Execution
+// is two launches per tile of Bluestein rows: k_twiddle_sum (pass 1) and
+// k_bluestein_rows (convolution + R2C writer).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gbspfft.h"
+#include "gbsp_internal.h"
+#include "gbsp_kernels.cuh"
+
+using gbsp::set_error;
+
+struct gbsp_plan_s {
+    int device = 0;
+    int rows = 0, cols = 0, nnz = 0, n_active = 0;
+    int L = 0, K = 1, Lp = 0;
+    gbsp::FFTDesc fd{};
+    int half_rows = 0, u_tile = 0, out_cols = 0, out_pitch = 0;
+    int idx_bytes = 2, tab_half = 0, big = 0, kahan_min = 64, ntab = 0;
+    int* d_col_ptr = nullptr;
+    void* d_row_idx = nullptr;
+    int* d_sparse_cols = nullptr;
+    float2* d_rowtab = nullptr;
+    float2* d_pre = nullptr;
+    float2* d_post = nullptr;
+    float2* d_filt = nullptr;
+    float2* d_fftw = nullptr;
+    float2* d_S = nullptr;
+    size_t s_pitch = 0;
+    int p1_threads = 512, p1_grid = 0;
+    size_t p1_smem = 0;
+    int rows_grid = 0;
+    size_t rows_smem = 0;
+    size_t device_bytes = 0;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+#define GB_CUDA(call)                                                                     \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return set_error(e_ == cudaErrorMemoryAllocation ? GBSP_ERR_ALLOC : GBSP_ERR_CUDA, \
+                             std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+int dev_alloc(gbsp_plan_s* p, void** ptr, size_t bytes) {
+    bytes = std::max<size_t>(bytes, 16);
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(GBSP_ERR_ALLOC, std::string("cudaMalloc(") + std::to_string(bytes) +
+                                             "): " + cudaGetErrorString(e));
+    }
+    p->allocs.push_back(*ptr);
+    p->device_bytes += bytes;
+    return GBSP_OK;
+}
+
+void free_plan(gbsp_plan_s* p) {
+    if (!p) return;
+    for (void* a : p->allocs) cudaFree(a);
+    delete p;
+}
+
+inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// Radix plan for a 7-smooth channel length: radix-8 stages while three or
+// more factors of 2 remain, then 4 or 2, then 3s, 5s and 7s.
+int build_fft_desc(int Lp, gbsp::FFTDesc* fd) {
+    int e2 = 0, e3 = 0, e5 = 0, e7 = 0, x = Lp;
+    while (x % 2 == 0) { x /= 2; e2++; }
+    while (x % 3 == 0) { x /= 3; e3++; }
+    while (x % 5 == 0) { x /= 5; e5++; }
+    while (x % 7 == 0) { x /= 7; e7++; }
+    if (x != 1) return GBSP_ERR_UNSUPPORTED;
+    std::vector<int> rs;
+    while (e2 >= 3) { rs.push_back(8); e2 -= 3; }
+    if (e2 == 2) rs.push_back(4);
+    if (e2 == 1) rs.push_back(2);
+    for (int i = 0; i < e3; i++) rs.push_back(3);
+    for (int i = 0; i < e5; i++) rs.push_back(5);
+    for (int i = 0; i < e7; i++) rs.push_back(7);
+    if ((int)rs.size() > gbsp::MAX_STAGES || rs.empty()) return GBSP_ERR_UNSUPPORTED;
+    fd->Lp = Lp;
+    fd->nst = (int)rs.size();
+    int l = 1, off = 0;
+    for (int s = 0; s < fd->nst; s++) {
+        const int R = rs[s];
+        const int m = Lp / (l * R);
+        fd->R[s] = R;
+        fd->m[s] = m;
+        fd->magic[s] = (m <= 1) ? 0u : (uint32_t)(((1ull << 32) + (uint64_t)m - 1) / (uint64_t)m);
+        fd->twoff[s] = off;
+        off += (R - 1) * m;
+        l *= R;
+    }
+    return GBSP_OK;
+}
+
+int fft_tw_count(const gbsp::FFTDesc& fd) {
+    int n = 0;
+    for (int s = 0; s < fd.nst; s++) n += (fd.R[s] - 1) * fd.m[s];
+    return n;
+}
+
+template <typename IDX, bool HALF, bool BIG>
+int set_pass1_attr(size_t smem) {
+    GB_CUDA(cudaFuncSetAttribute(gbsp::k_twiddle_sum<IDX, HALF, BIG>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return GBSP_OK;
+}
+
+template <typename IDX, bool HALF, bool BIG>
+int occ_pass1(int threads, size_t smem, int* nb) {
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, gbsp::k_twiddle_sum<IDX, HALF, BIG>,
+                                                          threads, smem));
+    return GBSP_OK;
+}
+
+template <typename IDX, bool HALF, bool BIG>
+void launch_pass1_t(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pitch,
+                    cudaStream_t st) {
+    gbsp::k_twiddle_sum<IDX, HALF, BIG><<<p->p1_grid, p->p1_threads, p->p1_smem, st>>>(
+        p->d_col_ptr, (const IDX*)p->d_row_idx, p->n_active, p->d_rowtab, p->ntab, p->rows,
+        1.0f / (float)p->rows, u0, n, S, s_pitch, p->kahan_min);
+}
+
+template <bool HALF, bool BIG>
+int pass1_dispatch_idx(const gbsp_plan_s* p, int what, int u0, int n, float2* S, size_t sp,
+                       cudaStream_t st, size_t smem, int threads, int* nb) {
+    if (p->idx_bytes == 2) {
+        if (what == 0) return set_pass1_attr<uint16_t, HALF, BIG>(smem);
+        if (what == 1) return occ_pass1<uint16_t, HALF, BIG>(threads, smem, nb);
+        launch_pass1_t<uint16_t, HALF, BIG>(p, u0, n, S, sp, st);
+    } else {
+        if (what == 0) return set_pass1_attr<uint32_t, HALF, BIG>(smem);
+        if (what == 1) return occ_pass1<uint32_t, HALF, BIG>(threads, smem, nb);
+        launch_pass1_t<uint32_t, HALF, BIG>(p, u0, n, S, sp, st);
+    }
+    return GBSP_OK;
+}
+
+// what: 0 = set smem attribute, 1 = occupancy query, 2 = launch
+int pass1_dispatch(const gbsp_plan_s* p, int what, int u0, int n, float2* S, size_t sp,
+                   cudaStream_t st, size_t smem = 0, int threads = 0, int* nb = nullptr) {
+    if (p->tab_half) {
+        if (p->big) return pass1_dispatch_idx<true, true>(p, what, u0, n, S, sp, st, smem, threads, nb);
+        return pass1_dispatch_idx<true, false>(p, what, u0, n, S, sp, st, smem, threads, nb);
+    }
+    if (p->big) return pass1_dispatch_idx<false, true>(p, what, u0, n, S, sp, st, smem, threads, nb);
+    return pass1_dispatch_idx<false, false>(p, what, u0, n, S, sp, st, smem, threads, nb);
+}
+
+int launch_rows(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch,
+                cudaStream_t st) {
+    if (p->K == 1) {
+        gbsp::k_bluestein_rows<false><<<p->rows_grid, gbsp::ROWS_THREADS, p->rows_smem, st>>>(
+            p->d_S, p->s_pitch, p->n_active, p->d_sparse_cols, p->d_pre, p->d_post, p->d_filt,
+            p->d_fftw, p->fd, 1, p->rows, p->cols, u0, n, (float2*)d_out, out_pitch);
+        return GBSP_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    cfg.gridDim = dim3(p->rows_grid);
+    cfg.blockDim = dim3(gbsp::ROWS_THREADS);
+    cfg.dynamicSmemBytes = p->rows_smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = p->K;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<true>, (const float2*)p->d_S,
+                               p->s_pitch, p->n_active, (const int*)p->d_sparse_cols,
+                               (const float2*)p->d_pre, (const float2*)p->d_post,
+                               (const float2*)p->d_filt, (const float2*)p->d_fftw, p->fd, p->K,
+                               p->rows, p->cols, u0, n, (float2*)d_out, out_pitch));
+    return GBSP_OK;
+}
+
+int validate_csc(int rows, int cols, int n_active, int nnz, const int* col_ptr,
+                 const int* row_idx, const int* sparse_cols) {
+    if (rows < 1 || cols < 1 || nnz < 0 || n_active < 0 || n_active > cols)
+        return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: bad sizes");
+    if (!col_ptr || (n_active > 0 && !sparse_cols) || (nnz > 0 && !row_idx))
+        return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: null CSC array");
+    if (col_ptr[0] != 0 || col_ptr[n_active] != nnz)
+        return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: col_ptr must run from 0 to nnz");
+    for (int j = 0; j < n_active; j++) {
+        if (col_ptr[j + 1] < col_ptr[j])
+            return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: col_ptr not monotone");
+        if (sparse_cols[j] < 0 || sparse_cols[j] >= cols || (j > 0 && sparse_cols[j] <= sparse_cols[j - 1]))
+            return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: sparse_cols not strictly increasing in [0,cols)");
+    }
+    for (int i = 0; i < nnz; i++)
+        if (row_idx[i] < 0 || row_idx[i] >= rows)
+            return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: row index out of range");
+    return GBSP_OK;
+}
+
+int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int* sparse_cols,
+               const gbsp_options* o, cudaStream_t st) {
+    const int policy = (o && o->length_policy) ? o->length_policy : GBSP_LEN_3SMOOTH;
+    if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH)
+        return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: length_policy must be 3 or 7");
+    GB_CUDA(cudaGetDevice(&p->device));
+    cudaDeviceProp prop;
+    GB_CUDA(cudaGetDeviceProperties(&prop, p->device));
+    const size_t smem_cap = prop.sharedMemPerBlockOptin;
+
+    // ---- lengths and channel split
+    long L = gbsp::next_smooth(2L * p->cols - 1, policy);
+    if (L < 2) L = 2;
+    if (L > (1L << 28)) return set_error(GBSP_ERR_UNSUPPORTED, "fft_len too large");
+    p->L = (int)L;
+    int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 20736;
+    maxLp = std::min<long>(maxLp, (long)(smem_cap / sizeof(float2)));
+    p->K = 0;
+    for (int k = 1; k <= gbsp::MAX_CHANNELS; k++) {
+        if (L % k == 0 && L / k <= maxLp && L / k >= 2) { p->K = k; break; }
+    }
+    if (p->K == 0)
+        return set_error(GBSP_ERR_UNSUPPORTED,
+                         "fft_len " + std::to_string(L) + " does not split into <= 8 channels of <= " +
+                             std::to_string(maxLp));
+    p->Lp = (int)(L / p->K);
+    if (build_fft_desc(p->Lp, &p->fd) != GBSP_OK)
+        return set_error(GBSP_ERR_UNSUPPORTED, "channel length has no radix plan");
+
+    p->half_rows = p->rows / 2 + 1;
+    p->out_cols = p->cols / 2 + 1;
+    p->out_pitch = (p->out_cols + 3) / 4 * 4;
+    p->u_tile = (o && o->u_tile > 0) ? std::min(o->u_tile, p->half_rows) : p->half_rows;
+    p->kahan_min = (o && o->kahan_min_degree != 0) ? o->kahan_min_degree : 64;
+    if (p->kahan_min < 0) p->kahan_min = 0;  // 0 disables compensation in the kernel
+    int ib = (o && o->index_bytes) ? o->index_bytes : ((p->rows <= 65536 && p->cols <= 65536) ? 2 : 4);
+    if (ib != 2 && ib != 4) return set_error(GBSP_ERR_INVALID, "index_bytes must be 2 or 4");
+    if (ib == 2 && p->rows > 65536) return set_error(GBSP_ERR_INVALID, "rows > 65536 need 4-byte indices");
+    p->idx_bytes = ib;
+    p->big = p->rows > 65535;
+
+    // ---- pass-1 configuration: twiddle table in shared memory
+    const size_t tab_budget = smem_cap - 1024;
+    if ((size_t)p->rows * sizeof(float2) <= std::min<size_t>(tab_budget, 160 * 1024)) {
+        p->tab_half = 0;
+        p->ntab = p->rows;
+    } else if ((size_t)(p->rows / 2 + 1) * sizeof(float2) <= tab_budget) {
+        p->tab_half = 1;
+        p->ntab = p->rows / 2 + 1;
+    } else {
+        return set_error(GBSP_ERR_UNSUPPORTED, "rows too large for a shared-memory twiddle table");
+    }
+    p->p1_threads = (o && o->pass1_threads > 0) ? o->pass1_threads : 512;
+    if (p->p1_threads % 32 || p->p1_threads > 512)
+        return set_error(GBSP_ERR_INVALID, "pass1_threads must be a multiple of 32, <= 512");
+    p->p1_smem = (size_t)p->ntab * sizeof(float2);
+    {
+        int rc = pass1_dispatch(p, 0, 0, 0, nullptr, 0, st, p->p1_smem);
+        if (rc) return rc;
+        int nb = 0;
+        rc = pass1_dispatch(p, 1, 0, 0, nullptr, 0, st, p->p1_smem, p->p1_threads, &nb);
+        if (rc) return rc;
+        if (nb < 1) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 kernel does not fit on an SM");
+        p->p1_grid = nb * prop.multiProcessorCount;
+    }
+
+    // ---- row-kernel configuration
+    p->rows_smem = (size_t)p->Lp * sizeof(float2);
+    if (p->K == 1) {
+        GB_CUDA(cudaFuncSetAttribute(gbsp::k_bluestein_rows<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->rows_smem));
+        int nb = 0;
+        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gbsp::k_bluestein_rows<false>,
+                                                              gbsp::ROWS_THREADS, p->rows_smem));
+        if (nb < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row kernel does not fit on an SM");
+        p->rows_grid = nb * prop.multiProcessorCount;
+    } else {
+        GB_CUDA(cudaFuncSetAttribute(gbsp::k_bluestein_rows<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->rows_smem));
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        cfg.gridDim = dim3(p->K * prop.multiProcessorCount);
+        cfg.blockDim = dim3(gbsp::ROWS_THREADS);
+        cfg.dynamicSmemBytes = p->rows_smem;
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = p->K;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int ncl = 0;
+        GB_CUDA(cudaOccupancyMaxActiveClusters(&ncl, gbsp::k_bluestein_rows<true>, &cfg));
+        if (ncl < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row-kernel cluster does not fit");
+        p->rows_grid = ncl * p->K;
+    }
+
+    // ---- uploads
+    const int na = p->n_active;
+    int rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_col_ptr, (size_t)(na + 1) * sizeof(int)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_sparse_cols, (size_t)std::max(na, 1) * sizeof(int)))) return rc;
+    if ((rc = dev_alloc(p, &p->d_row_idx, (size_t)std::max(p->nnz, 1) * p->idx_bytes))) return rc;
+    GB_CUDA(cudaMemcpyAsync(p->d_col_ptr, col_ptr, (size_t)(na + 1) * sizeof(int),
+                            cudaMemcpyHostToDevice, st));
+    if (na > 0)
+        GB_CUDA(cudaMemcpyAsync(p->d_sparse_cols, sparse_cols, (size_t)na * sizeof(int),
+                                cudaMemcpyHostToDevice, st));
+    std::vector<uint16_t> r16;
+    if (p->nnz > 0) {
+        if (p->idx_bytes == 2) {
+            r16.resize(p->nnz);
+            for (int i = 0; i < p->nnz; i++) r16[i] = (uint16_t)row_idx[i];
+            GB_CUDA(cudaMemcpyAsync(p->d_row_idx, r16.data(), (size_t)p->nnz * 2,
+                                    cudaMemcpyHostToDevice, st));
+        } else {
+            GB_CUDA(cudaMemcpyAsync(p->d_row_idx, row_idx, (size_t)p->nnz * 4,
+                                    cudaMemcpyHostToDevice, st));
+        }
+    }
+
+    // ---- tables (FP64 on the device, rounded to FP32)
+    const int K = p->K, Lp = p->Lp, cols = p->cols;
+    if ((rc = dev_alloc(p, (void**)&p->d_rowtab, (size_t)p->ntab * sizeof(float2)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_pre, (size_t)K * cols * sizeof(float2)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_post, (size_t)K * cols * sizeof(float2)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_filt, (size_t)K * Lp * sizeof(float2)))) return rc;
+    const int ntw = std::max(fft_tw_count(p->fd), 1);
+    if ((rc = dev_alloc(p, (void**)&p->d_fftw, (size_t)ntw * sizeof(float2)))) return rc;
+
+    gbsp::k_table_rows<<<blocks_for(p->ntab, 256), 256, 0, st>>>(p->d_rowtab, p->ntab, p->rows);
+    GB_CUDA(cudaGetLastError());
+    gbsp::k_table_chirp<<<blocks_for((long)K * cols, 256), 256, 0, st>>>(p->d_pre, p->d_post, cols,
+                                                                          p->L, K);
+    GB_CUDA(cudaGetLastError());
+    for (int s = 0; s < p->fd.nst; s++) {
+        const int n = (p->fd.R[s] - 1) * p->fd.m[s];
+        gbsp::k_table_fft<<<blocks_for(n, 256), 256, 0, st>>>(p->d_fftw, Lp, p->fd.R[s], p->fd.m[s],
+                                                               p->fd.twoff[s]);
+        GB_CUDA(cudaGetLastError());
+    }
+    double2* d_spec = nullptr;
+    GB_CUDA(cudaMalloc((void**)&d_spec, (size_t)K * Lp * sizeof(double2)));
+    gbsp::k_table_filter_input<<<blocks_for((long)K * Lp, 256), 256, 0, st>>>(d_spec, cols, p->L, K, Lp);
+    cudaError_t e = cudaGetLastError();
+    for (int s = 0; s < p->fd.nst && e == cudaSuccess; s++) {
+        const long nbf = (long)K * (Lp / p->fd.R[s]);
+        gbsp::k_dif_stage_f64<<<blocks_for(nbf, 128), 128, 0, st>>>(d_spec, K, Lp, p->fd.R[s], p->fd.m[s]);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        gbsp::k_table_filter_final<<<blocks_for((long)K * Lp, 256), 256, 0, st>>>(
+            p->d_filt, d_spec, (long)K * Lp, 1.0 / (double)p->L);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_spec);
+    if (e != cudaSuccess)
+        return set_error(GBSP_ERR_CUDA, std::string("plan tables: ") + cudaGetErrorString(e));
+
+    // ---- pass-1 scratch tile
+    p->s_pitch = (size_t)std::max(na, 1);
+    p->s_pitch = (p->s_pitch + 1) & ~(size_t)1;
+    if ((rc = dev_alloc(p, (void**)&p->d_S, (size_t)p->u_tile * p->s_pitch * sizeof(float2)))) return rc;
+    return GBSP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbsp_plan_create(int rows, int cols, int n_active, int nnz, const int* col_ptr,
+                     const int* row_idx, const int* sparse_cols, const gbsp_options* opts,
+                     void* stream, gbsp_plan_t* plan) {
+    if (!plan) return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: plan is null");
+    *plan = nullptr;
+    int rc = validate_csc(rows, cols, n_active, nnz, col_ptr, row_idx, sparse_cols);
+    if (rc) return rc;
+    gbsp_plan_s* p = new (std::nothrow) gbsp_plan_s();
+    if (!p) return set_error(GBSP_ERR_ALLOC, "gbsp_plan_create: out of host memory");
+    p->rows = rows;
+    p->cols = cols;
+    p->nnz = nnz;
+    p->n_active = n_active;
+    rc = plan_build(p, col_ptr, row_idx, sparse_cols, opts, (cudaStream_t)stream);
+    if (rc) {
+        free_plan(p);
+        return rc;
+    }
+    *plan = p;
+    return GBSP_OK;
+}
+
+int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
+    if (!p || !info) return set_error(GBSP_ERR_INVALID, "gbsp_plan_get_info: null argument");
+    std::memset(info, 0, sizeof(*info));
+    info->rows = p->rows;
+    info->cols = p->cols;
+    info->nnz = p->nnz;
+    info->n_active = p->n_active;
+    info->fft_len = p->L;
+    info->channels = p->K;
+    info->channel_len = p->Lp;
+    info->n_stages = p->fd.nst;
+    for (int s = 0; s < p->fd.nst; s++) info->radix[s] = p->fd.R[s];
+    info->output_cols = p->out_cols;
+    info->output_pitch = p->out_pitch;
+    info->half_rows = p->half_rows;
+    info->u_tile = p->u_tile;
+    info->index_bytes = p->idx_bytes;
+    info->row_table_mode = p->tab_half;
+    info->device_bytes = p->device_bytes;
+    return GBSP_OK;
+}
+
+int gbsp_plan_destroy(gbsp_plan_t p) {
+    free_plan(p);
+    return GBSP_OK;
+}
+
+int gbsp_execute(gbsp_plan_t p, void* d_out, size_t out_pitch, void* stream) {
+    if (!p || !d_out) return set_error(GBSP_ERR_INVALID, "gbsp_execute: null argument");
+    if (out_pitch < (size_t)p->out_cols || (out_pitch & 1))
+        return set_error(GBSP_ERR_INVALID, "gbsp_execute: out_pitch must be even and >= cols/2+1");
+    if (((uintptr_t)d_out & 15) != 0)
+        return set_error(GBSP_ERR_INVALID, "gbsp_execute: d_out must be 16-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int u0 = 0; u0 < p->half_rows; u0 += p->u_tile) {
+        const int n = std::min(p->u_tile, p->half_rows - u0);
+        pass1_dispatch(p, 2, u0, n, p->d_S, p->s_pitch, st);
+        GB_CUDA(cudaGetLastError());
+        int rc = launch_rows(p, u0, n, d_out, out_pitch, st);
+        if (rc) return rc;
+        GB_CUDA(cudaGetLastError());
+    }
+    return GBSP_OK;
+}
+
+int gbsp_column_sums(gbsp_plan_t p, int u0, int n_rows, void* d_s, size_t s_pitch, void* stream) {
+    if (!p || !d_s) return set_error(GBSP_ERR_INVALID, "gbsp_column_sums: null argument");
+    if (u0 < 0 || n_rows < 1 || u0 + n_rows > p->rows ||
+        s_pitch < (size_t)std::max(p->n_active, 1))
+        return set_error(GBSP_ERR_INVALID, "gbsp_column_sums: bad range or pitch");
+    pass1_dispatch(p, 2, u0, n_rows, (float2*)d_s, s_pitch, (cudaStream_t)stream);
+    GB_CUDA(cudaGetLastError());
+    return GBSP_OK;
+}
+
+}  // extern "C"

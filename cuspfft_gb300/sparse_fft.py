@@ -1,0 +1,194 @@
+"""Python mirror of the reference's sparse FFT interface over the C ABI.
+
+Names, argument meanings and error behaviour follow the reference's C++ API
+(include/sparse_fft.h:7-83, include/mtx_reader.h:7-30,
+include/sparse_fft_internal.cuh:193-222); every call goes through
+libgbspfft.so (include/gbspfft.h).  torch supplies device memory and streams.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import _capi
+from ._capi import GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GbspOptions, GbspPlanInfo, check, load
+
+
+@dataclass
+class COOMatrix:
+    """Binary sparse matrix: (row, col) pairs, values implicitly 1."""
+    rows: int
+    cols: int
+    row_idx: np.ndarray
+    col_idx: np.ndarray
+
+    def __post_init__(self):
+        self.row_idx = np.ascontiguousarray(self.row_idx, dtype=np.int32)
+        self.col_idx = np.ascontiguousarray(self.col_idx, dtype=np.int32)
+        if self.row_idx.shape != self.col_idx.shape or self.row_idx.ndim != 1:
+            raise ValueError("row_idx and col_idx must be 1-D arrays of equal length")
+
+    @property
+    def nnz(self) -> int:
+        return int(self.row_idx.size)
+
+
+@dataclass
+class CompactCSC:
+    n_sparse_cols: int
+    sparse_cols: np.ndarray
+    col_ptr: np.ndarray
+    row_idx: np.ndarray
+
+
+@dataclass
+class SparseFFTResult:
+    """d_output: torch complex64 tensor (rows, output_cols) on the GPU;
+    output_cols is the padded row pitch (cols/2+1 rounded up to 4)."""
+    d_output: object
+    output_cols: int
+    ms: float
+    mem_bytes: int
+    h_output: list = field(default_factory=list)
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def read_mtx(path: str) -> COOMatrix:
+    """Binarizing Matrix Market reader; raises RuntimeError on failure
+    (the reference throws std::runtime_error, src/mtx_reader.cu:7-77)."""
+    lib = load()
+    rows, cols, nnz = C.c_int(), C.c_int(), C.c_int()
+    ri, ci = C.POINTER(C.c_int)(), C.POINTER(C.c_int)()
+    st = lib.gbsp_read_mtx(str(path).encode(), C.byref(rows), C.byref(cols), C.byref(nnz),
+                           C.byref(ri), C.byref(ci))
+    if st != 0:
+        raise RuntimeError(_capi.last_error())
+    try:
+        n = nnz.value
+        r = np.ctypeslib.as_array(ri, shape=(max(n, 1),))[:n].copy()
+        c = np.ctypeslib.as_array(ci, shape=(max(n, 1),))[:n].copy()
+    finally:
+        lib.gbsp_free(C.cast(ri, C.c_void_p))
+        lib.gbsp_free(C.cast(ci, C.c_void_p))
+    return COOMatrix(rows.value, cols.value, r, c)
+
+
+def make_compact_csc(coo: COOMatrix) -> CompactCSC:
+    lib = load()
+    sc = np.zeros(max(coo.cols, 1), np.int32)
+    cp = np.zeros(coo.cols + 1, np.int32)
+    ri = np.zeros(max(coo.nnz, 1), np.int32)
+    na = C.c_int()
+    check(lib.gbsp_build_compact_csc(coo.rows, coo.cols, coo.nnz, _ip(coo.row_idx), _ip(coo.col_idx),
+                                     C.byref(na), _ip(sc), _ip(cp), _ip(ri)), "make_compact_csc")
+    n = na.value
+    return CompactCSC(n, sc[:n].copy(), cp[:n + 1].copy(), ri[:coo.nnz].copy())
+
+
+def next_smooth(n: int, policy: int = GBSP_LEN_3SMOOTH) -> int:
+    return int(load().gbsp_next_smooth(int(n), int(policy)))
+
+
+def _stream_handle(stream) -> Optional[int]:
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return stream.cuda_stream
+
+
+class Plan:
+    """One matrix's transform: tables and uploaded CSC live on the GPU until
+    close().  execute() is the reference's timed tile loop."""
+
+    def __init__(self, coo: COOMatrix, *, length_policy: int = GBSP_LEN_3SMOOTH, u_tile: int = 0,
+                 kahan_min_degree: int = 0, index_bytes: int = 0, max_channel_len: int = 0,
+                 pass1_threads: int = 0, stream=None, csc: Optional[CompactCSC] = None):
+        lib = load()
+        self._lib = lib
+        self._h = C.c_void_p()
+        csc = csc if csc is not None else make_compact_csc(coo)
+        self.rows, self.cols = coo.rows, coo.cols
+        o = GbspOptions(length_policy=length_policy, u_tile=u_tile, kahan_min_degree=kahan_min_degree,
+                        index_bytes=index_bytes, max_channel_len=max_channel_len,
+                        pass1_threads=pass1_threads)
+        cp = np.ascontiguousarray(csc.col_ptr, np.int32)
+        ri = np.ascontiguousarray(csc.row_idx if coo.nnz else np.zeros(1, np.int32), np.int32)
+        sc = np.ascontiguousarray(csc.sparse_cols if csc.n_sparse_cols else np.zeros(1, np.int32),
+                                  np.int32)
+        check(lib.gbsp_plan_create(coo.rows, coo.cols, csc.n_sparse_cols, coo.nnz, _ip(cp), _ip(ri),
+                                   _ip(sc), C.byref(o), _stream_handle(stream), C.byref(self._h)),
+              "gbsp_plan_create")
+        info = GbspPlanInfo()
+        check(lib.gbsp_plan_get_info(self._h, C.byref(info)), "gbsp_plan_get_info")
+        self.info = info.as_dict()
+
+    @property
+    def output_pitch(self) -> int:
+        return self.info["output_pitch"]
+
+    def empty_output(self):
+        import torch
+        return torch.empty((self.rows, self.output_pitch), dtype=torch.complex64, device="cuda")
+
+    def execute(self, out, stream=None) -> None:
+        if out.dtype.__str__() != "torch.complex64" or not out.is_cuda or not out.is_contiguous():
+            raise ValueError("out must be a contiguous complex64 CUDA tensor")
+        if out.dim() != 2 or out.shape[0] < self.rows:
+            raise ValueError("out must have shape (rows, pitch)")
+        check(self._lib.gbsp_execute(self._h, C.c_void_p(out.data_ptr()), out.shape[1],
+                                     _stream_handle(stream)), "gbsp_execute")
+
+    def column_sums(self, u0: int, n_rows: int, out, stream=None) -> None:
+        check(self._lib.gbsp_column_sums(self._h, u0, n_rows, C.c_void_p(out.data_ptr()), out.shape[1],
+                                         _stream_handle(stream)), "gbsp_column_sums")
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.gbsp_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _run_method(coo: COOMatrix, u_tile: int, policy: int) -> SparseFFTResult:
+    import torch
+    if u_tile <= 0:
+        raise RuntimeError("CSC tile size must be positive")
+    free0, _ = torch.cuda.mem_get_info()
+    with Plan(coo, length_policy=policy, u_tile=u_tile) as plan:
+        out = plan.empty_output()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plan.execute(out)
+        e1.record()
+        e1.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        return SparseFFTResult(out, plan.output_pitch, e0.elapsed_time(e1), max(0, free0 - free1))
+
+
+def sparse_fft_csc_bluestein_mixed_radix(coo: COOMatrix, u_tile: int = 128) -> SparseFFTResult:
+    """Reference include/sparse_fft.h:57 -- fft_len = next 3-smooth >= 2*cols-1."""
+    return _run_method(coo, u_tile, GBSP_LEN_3SMOOTH)
+
+
+def sparse_fft_csc_bluestein_cufft_smooth(coo: COOMatrix, u_tile: int = 128) -> SparseFFTResult:
+    """Reference include/sparse_fft.h:70 -- fft_len = next 7-smooth >= 2*cols-1,
+    computed by this library's own FFT (no cuFFT)."""
+    return _run_method(coo, u_tile, GBSP_LEN_7SMOOTH)

@@ -1,0 +1,142 @@
+/*
+ * gbspfft.h -- C ABI of the GB300-native binary-sparse 2-D R2C FFT.
+ *
+ * Plain pointers, sizes and int status codes only: no C++ types, no torch
+ * types, no exceptions cross this boundary.  The C++ drop-in layer
+ * (include/sparse_fft.h, include/mtx_reader.h) and the Python package are
+ * both written on top of these entry points.
+ *
+ * What is computed (same as the reference's two hot methods,
+ * src/sparse_fft_bluestein.cu:2256-2392 and :2557-2719):
+ *   F[u][v] = sum over nonzeros (r,c) of exp(-2*pi*i*(r*u/rows + c*v/cols))
+ * for u in [0,rows), v in [0, cols/2], written row-major as complex64
+ * (interleaved float re, im) with a caller-chosen row pitch.
+ *
+ * All functions return GBSP_OK (0) on success or a positive GBSP_ERR_* code;
+ * gbsp_last_error() returns a message for the calling thread's last failure.
+ */
+#ifndef GBSPFFT_H
+#define GBSPFFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GBSP_OK = 0,
+    GBSP_ERR_INVALID = 1,     /* bad argument (sizes, pointers, options)      */
+    GBSP_ERR_CUDA = 2,        /* a CUDA runtime call or kernel launch failed  */
+    GBSP_ERR_ALLOC = 3,       /* device or host allocation failed             */
+    GBSP_ERR_UNSUPPORTED = 4, /* shape outside what this build handles        */
+    GBSP_ERR_IO = 5,          /* file could not be opened / parsed            */
+    GBSP_ERR_NOT_BUILT = 6    /* entry point exists for link compatibility only */
+};
+
+/* Length policy of the Bluestein convolution along the column axis.
+ *   GBSP_LEN_3SMOOTH: fft_len = next 2^a*3^b >= 2*cols-1
+ *                     (reference: next_3_smooth, src/sparse_fft_bluestein.cu:1975-1982,
+ *                      used by sparse_fft_csc_bluestein_mixed_radix)
+ *   GBSP_LEN_7SMOOTH: fft_len = next 2^a*3^b*5^c*7^d >= 2*cols-1
+ *                     (reference: next_7_smooth, :1987-1994,
+ *                      used by sparse_fft_csc_bluestein_cufft_smooth) */
+enum { GBSP_LEN_3SMOOTH = 3, GBSP_LEN_7SMOOTH = 7 };
+
+typedef struct gbsp_plan_s* gbsp_plan_t;
+
+/* Tuning knobs.  Zero-initialise and set what you need; 0 means "default".
+ * None of them changes the computed spectrum beyond FP32 rounding. */
+typedef struct {
+    int length_policy;     /* GBSP_LEN_3SMOOTH (default) or GBSP_LEN_7SMOOTH            */
+    int u_tile;            /* Bluestein rows per tile (each yields output rows u and
+                              rows-u); the --csc-tile analogue. 0 = all rows in one tile */
+    int kahan_min_degree;  /* columns with >= this many nonzeros accumulate with Kahan
+                              compensation; 0 = default 64; negative = never (plain FP32) */
+    int index_bytes;       /* 0 = auto (2 when rows,cols <= 65536, else 4), or 2 / 4      */
+    int max_channel_len;   /* largest per-CTA FFT length held in shared memory;
+                              0 = default; longer convolutions split into channels that
+                              run as one thread-block cluster                             */
+    int pass1_threads;     /* 0 = default (512)                                          */
+    int reserved[8];
+} gbsp_options;
+
+typedef struct {
+    int rows, cols, nnz, n_active;
+    int fft_len;           /* Bluestein convolution length L                              */
+    int channels;          /* K: L = K * channel_len, one CTA per channel                 */
+    int channel_len;       /* per-CTA FFT length held in shared memory                    */
+    int n_stages;          /* radix stages of the channel FFT                             */
+    int radix[16];         /* radix of each stage, first to last                          */
+    int output_cols;       /* cols/2 + 1                                                  */
+    int output_pitch;      /* row pitch (complex elements) the reference returns:
+                              (cols/2+1) rounded up to a multiple of 4                    */
+    int half_rows;         /* rows/2 + 1 Bluestein rows (Hermitian pairing)              */
+    int u_tile;            /* effective Bluestein rows per tile                           */
+    int index_bytes;       /* 2 or 4                                                      */
+    int row_table_mode;    /* 0 full twiddle table in shared memory, 1 half table        */
+    size_t device_bytes;   /* device memory held by the plan                              */
+} gbsp_plan_info;
+
+int         gbsp_version(void);
+const char* gbsp_status_string(int status);
+/* Copies the calling thread's last error message into buf (NUL-terminated). */
+int         gbsp_last_error(char* buf, size_t buflen);
+
+/* ---- host-side input path ------------------------------------------------
+ * Binarizing Matrix Market reader.  Replaces read_mtx
+ * (reference src/mtx_reader.cu:7-77, declared include/mtx_reader.h:18):
+ * coordinate header, "symmetric" substring => mirror off-diagonal entries,
+ * values ignored, 1-based -> 0-based, (row,col) pairs sorted and
+ * de-duplicated.  *row_idx / *col_idx are allocated by the library and
+ * released with gbsp_free(). */
+int gbsp_read_mtx(const char* path, int* rows, int* cols, int* nnz,
+                  int** row_idx, int** col_idx);
+void gbsp_free(void* p);
+
+/* Compact CSC over the active (non-empty) columns.  Replaces
+ * make_compact_csc (reference include/sparse_fft_internal.cuh:193-222):
+ * sparse_cols = sorted unique columns, col_ptr over active columns
+ * (n_active+1 entries), row_idx a stable counting sort of the COO order.
+ * Capacities: sparse_cols >= cols, col_ptr >= cols+1, row_idx_out >= nnz. */
+int gbsp_build_compact_csc(int rows, int cols, int nnz,
+                           const int* coo_row, const int* coo_col,
+                           int* n_active, int* sparse_cols, int* col_ptr,
+                           int* row_idx_out);
+
+/* Length policy helpers (same results as the reference's next_3_smooth /
+ * next_7_smooth, src/sparse_fft_bluestein.cu:1975-1994). */
+int gbsp_next_smooth(int n, int policy);
+
+/* ---- plans ---------------------------------------------------------------
+ * Builds every device table once (row twiddles, chirp, filter spectrum, FFT
+ * twiddles: FP64 on the GPU, rounded to FP32) and uploads the CSC.  Host
+ * arrays in, device state out; this is the reference's untimed setup
+ * (src/sparse_fft_bluestein.cu:2263-2321).  `stream` is a cudaStream_t
+ * (NULL = legacy default stream). */
+int gbsp_plan_create(int rows, int cols, int n_active, int nnz,
+                     const int* col_ptr, const int* row_idx, const int* sparse_cols,
+                     const gbsp_options* opts, void* stream, gbsp_plan_t* plan);
+int gbsp_plan_get_info(gbsp_plan_t plan, gbsp_plan_info* info);
+int gbsp_plan_destroy(gbsp_plan_t plan);
+
+/* Runs the transform: the reference's timed tile loop
+ * (src/sparse_fft_bluestein.cu:2327-2370).  d_out is device memory of at
+ * least rows*out_pitch complex64, 16-byte aligned; out_pitch >= cols/2+1 and
+ * even.  Columns [cols/2+1, out_pitch) are written as zeros.  Asynchronous
+ * on `stream`. */
+int gbsp_execute(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream);
+
+/* The pass-1 intermediate for inspection and tests: for Bluestein rows
+ * [u0, u0+n_rows) writes S[u][j] = sum_{r in column j} exp(-2*pi*i*u*r/rows)
+ * to d_s (complex64, row pitch s_pitch >= n_active).  n_rows <= the plan's
+ * u_tile.  This is the reference's csc_build_bluestein_input_*kernel
+ * (src/sparse_fft_bluestein.cu:334-397) before its chirp multiply. */
+int gbsp_column_sums(gbsp_plan_t plan, int u0, int n_rows, void* d_s, size_t s_pitch,
+                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBSPFFT_H */

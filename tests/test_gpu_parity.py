@@ -1,0 +1,165 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 oracle.
+
+Tolerance: relative L2 error <= 1e-5 over the whole half-spectrum, the bar
+the FP32 form must meet against a double-precision DFT of the same binary
+matrix.  Padding columns [cols/2+1, pitch) must be exactly zero.
+"""
+import numpy as np
+import pytest
+
+import cuspfft_gb300 as gb
+from cuspfft_gb300 import synthetic
+from oracle import fp64
+
+pytestmark = pytest.mark.gpu
+
+REL_L2_TOL = 1e-5
+
+
+def run_plan(coo, **kw):
+    import torch
+    with gb.Plan(coo, **kw) as plan:
+        out = plan.empty_output()
+        out.fill_(complex(7.0, 7.0))  # poison: every element must be overwritten
+        plan.execute(out)
+        torch.cuda.synchronize()
+        return out.cpu().numpy(), plan.info
+
+
+def check_against_oracle(coo, got, us=None, tol=REL_L2_TOL):
+    fc = coo.cols // 2 + 1
+    if us is None:
+        ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx)
+        sub = got[:, :fc]
+    else:
+        ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, us)
+        sub = got[us, :fc]
+    err = fp64.rel_l2(sub, ref)
+    assert err <= tol, f"rel-L2 {err:.3e} > {tol:.0e}"
+    assert np.all(got[:, fc:] == 0), "padding columns must be zero"
+    return err
+
+
+SHAPES = [(1, 1), (1, 7), (7, 1), (2, 2), (3, 5), (17, 31), (64, 64), (101, 97), (128, 250),
+          (255, 256), (300, 1001), (997, 13), (513, 2048)]
+
+
+@pytest.mark.parametrize("rows,cols", SHAPES)
+@pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH])
+def test_random_shapes(cuda, rows, cols, policy):
+    g = np.random.default_rng(rows * 1000 + cols)
+    n = max(1, int(0.05 * rows * cols))
+    coo = synthetic.normalise(rows, cols, g.integers(0, rows, n), g.integers(0, cols, n))
+    got, info = run_plan(coo, length_policy=policy)
+    check_against_oracle(coo, got)
+
+
+# cols = 333: 3-smooth L = 729 = 3^6, 7-smooth L = 672 = 2^5 * 3 * 7
+@pytest.mark.parametrize("policy,max_len,channels", [
+    (gb.GBSP_LEN_3SMOOTH, 250, 3), (gb.GBSP_LEN_7SMOOTH, 250, 3), (gb.GBSP_LEN_7SMOOTH, 340, 2),
+    (gb.GBSP_LEN_7SMOOTH, 170, 4), (gb.GBSP_LEN_7SMOOTH, 120, 6), (gb.GBSP_LEN_7SMOOTH, 100, 7),
+    (gb.GBSP_LEN_7SMOOTH, 84, 8)])
+def test_channel_split_clusters(cuda, policy, max_len, channels):
+    # forces the length-L convolution into K channels run as one thread-block cluster
+    g = np.random.default_rng(max_len)
+    rows, cols = 123, 333
+    coo = synthetic.normalise(rows, cols, g.integers(0, rows, 3000), g.integers(0, cols, 3000))
+    got, info = run_plan(coo, length_policy=policy, max_channel_len=max_len)
+    assert info["channels"] == channels
+    check_against_oracle(coo, got)
+
+
+def test_u_tiles_and_index_width(cuda):
+    coo = synthetic.uniform_matrix(257, 300, 4000, seed=9)
+    base, _ = run_plan(coo)
+    for kw in ({"u_tile": 1}, {"u_tile": 5}, {"u_tile": 64}, {"index_bytes": 4},
+               {"kahan_min_degree": 1}, {"kahan_min_degree": -1}, {"pass1_threads": 64}):
+        got, _ = run_plan(coo, **kw)
+        check_against_oracle(coo, got)
+        assert fp64.rel_l2(got, base) < 1e-5
+
+
+def test_half_row_table(cuda):
+    # rows beyond the full-table budget use the half-circle twiddle table
+    coo = synthetic.uniform_matrix(24001, 40, 20000, seed=11)
+    got, info = run_plan(coo)
+    assert info["row_table_mode"] == 1
+    check_against_oracle(coo, got)
+
+
+def test_known_answers(cuda):
+    rows, cols = 12, 10
+    # empty matrix -> all zeros
+    empty = gb.COOMatrix(rows, cols, np.zeros(0, np.int32), np.zeros(0, np.int32))
+    got, _ = run_plan(empty)
+    assert np.all(got == 0)
+    # one nonzero at (r0, c0): unit-modulus plane wave
+    r0, c0 = 5, 3
+    one = gb.COOMatrix(rows, cols, np.array([r0]), np.array([c0]))
+    got, _ = run_plan(one)
+    u = np.arange(rows)[:, None]
+    v = np.arange(cols // 2 + 1)[None, :]
+    expect = np.exp(-2j * np.pi * (u * r0 / rows + v * c0 / cols))
+    assert np.max(np.abs(got[:, : cols // 2 + 1] - expect)) < 1e-5
+    # a full matrix row: F[u][v] = cols * delta(v) * exp(-2 pi i u r0 / rows)
+    full = gb.COOMatrix(rows, cols, np.full(cols, r0), np.arange(cols))
+    got, _ = run_plan(full)
+    assert abs(got[0, 0] - cols) < 1e-4
+    assert np.max(np.abs(got[:, 1: cols // 2 + 1])) < 1e-4
+    # F[0][0] = nnz
+    coo = synthetic.uniform_matrix(50, 60, 700, seed=3)
+    got, _ = run_plan(coo)
+    assert abs(got[0, 0] - coo.nnz) < 1e-3 * coo.nnz
+
+
+def test_symmetric_transpose_property(cuda):
+    # A symmetric with rows == cols  =>  F[u][v] == F[v][u]
+    coo = synthetic.uniform_powerlaw(n=301, target_nnz=3000, seed=8)
+    got, _ = run_plan(coo)
+    h = coo.cols // 2 + 1
+    blk = got[:h, :h]
+    assert fp64.rel_l2(blk, blk.T) < 1e-5
+
+
+def test_column_sums(cuda):
+    import torch
+    coo = synthetic.uniform_matrix(211, 77, 2000, seed=5)
+    csc = gb.make_compact_csc(coo)
+    with gb.Plan(coo) as plan:
+        s = torch.zeros((20, csc.n_sparse_cols), dtype=torch.complex64, device="cuda")
+        plan.column_sums(30, 20, s)
+        torch.cuda.synchronize()
+        got = s.cpu().numpy()
+    ref = fp64.column_sums_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, np.arange(30, 50))
+    assert fp64.rel_l2(got, ref[:, csc.sparse_cols]) < 1e-6
+
+
+def test_config_uniform_3001x2048_full(cuda):
+    coo = synthetic.config_matrix("uniform_3001x2048")
+    for policy in (gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH):
+        got, info = run_plan(coo, length_policy=policy)
+        check_against_oracle(coo, got)
+
+
+@pytest.mark.parametrize("name", ["banded_powerlaw_8219", "uniform_powerlaw_16706"])
+def test_config_sampled_rows(cuda, name):
+    coo = synthetic.config_matrix(name)
+    g = np.random.default_rng(0)
+    us = np.unique(np.concatenate([[0, 1, coo.rows // 2, coo.rows - 1], g.integers(0, coo.rows, 12)]))
+    for policy in (gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH):
+        got, info = run_plan(coo, length_policy=policy)
+        check_against_oracle(coo, got, us=us)
+
+
+def test_reference_api_methods(cuda):
+    import torch
+    coo = synthetic.uniform_matrix(301, 127, 1500, seed=21)
+    ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx)
+    for fn in (gb.sparse_fft_csc_bluestein_mixed_radix, gb.sparse_fft_csc_bluestein_cufft_smooth):
+        res = fn(coo, 16)
+        assert res.output_cols == (coo.cols // 2 + 1 + 3) // 4 * 4
+        assert res.ms > 0
+        got = res.d_output.cpu().numpy()[:, : coo.cols // 2 + 1]
+        assert fp64.rel_l2(got, ref) < REL_L2_TOL
+    with pytest.raises(RuntimeError):
+        gb.sparse_fft_csc_bluestein_mixed_radix(coo, 0)
