@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Benchmark of the binary-sparse 2-D R2C FFT on one GB300 (N replicas under torchrun).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME] [--policy 3|7]
+
+One step = one full transform of the workload (pass 1 + Bluestein rows +
+R2C writer) on a synthetic binary matrix with the shape of the reference's
+benzene benchmark (8219 x 8219 symmetric, ~242k nnz, power-law degrees in a
+band).  Prints ONE JSON line (rank 0):
+
+  value        device ms per FFT with the CSC and tables resident (plan built
+               before the timed region), max over ranks / FFTs of all ranks
+  e2e          ms per FFT through the reference-style API with host buffers:
+               CSC from pinned host memory in, plan built, transform, full
+               spectrum read back to pinned host memory, plan released
+  roofline     the dominant kernel's achieved bytes and FLOPs vs measured peaks
+  cpu_baseline the reference's CPU path (dense float32 scatter + 2-D R2C FFT,
+               execute step only) on this host's cores, a bounded sample
+  accuracy     rel-L2 vs the FP64 oracle on sampled output rows
+
+L2 is flushed (a 512 MiB write) before every timed step, outside the events.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "banded_powerlaw_8219": "Symmetric binary adjacency 8219x8219, ~242k nnz, empty diagonal, power-law "
+                            "degrees, neighbours in a +-150 band; uint16 indices",
+    "uniform_powerlaw_16706": "Symmetric binary adjacency 16706x16706, ~396k nnz, power-law degrees, "
+                              "uniform neighbours; 1.1165 GB R2C output",
+    "uniform_3001x2048": "3001x2048 binary, 0.5% i.i.d. uniform positions",
+    "uniform_powerlaw_40421": "Symmetric binary adjacency 40421x40421, ~351k nnz, uint32 indices",
+}
+METRIC = "ms/FFT (binary-sparse 2-D R2C, rel-L2<=1e-5 vs FP64)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="banded_powerlaw_8219", choices=sorted(WORKLOADS))
+    ap.add_argument("--policy", type=int, default=7, choices=[3, 7])
+    ap.add_argument("--u-tile", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+def cpu_baseline(coo, budget: float) -> dict:
+    from oracle import ref_port
+    t = ref_port.time_cpu_baseline(coo.rows, coo.cols, coo.row_idx, coo.col_idx, budget_s=budget)
+    return {"value": round(t["ms_median"], 3), "unit": "ms/FFT", "cores": t["workers"], "kind": "port",
+            "sample": f"{t['reps']} full transforms of the workload; scipy.fft.rfft2 float32 (pocketfft) "
+                      f"standing in for FFTW fftwf_execute, workers={t['workers']}, execute step timed"}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference's CPU implementation of the path (its
+    FFTW 2-D R2C; restated with pocketfft, FFTW being absent) on all host cores."""
+    if rank != 0:
+        return 0
+    from cuspfft_gb300 import synthetic
+    from oracle import ref_port
+    coo = synthetic.config_matrix(args.workload)
+    ncores = os.cpu_count() or 1
+    times = []
+    for _ in range(max(args.warmup, 1)):
+        ref_port.cpu_fft_r2c_2d(coo.rows, coo.cols, coo.row_idx, coo.col_idx, workers=ncores)
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        _, ms = ref_port.cpu_fft_r2c_2d(coo.rows, coo.cols, coo.row_idx, coo.col_idx, workers=ncores)
+        times.append(ms)
+        if time.perf_counter() - t_start > 120:
+            break
+    ms = statistics.median(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 4), "unit": "ms/FFT", "n_gpus": args.gpus,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "shape": [coo.rows, coo.cols], "nnz": coo.nnz,
+                   "method": "dense float32 scatter + 2-D R2C FFT (reference cpu_fft_r2c_2d; "
+                             "pocketfft stand-in for FFTW)"},
+        "cpu_baseline": {"value": round(ms, 4), "unit": "ms/FFT", "cores": ncores, "kind": "port",
+                         "sample": f"{len(times)} full transforms, execute step timed"},
+        "e2e": {"value": round(ms, 4), "unit": "ms/FFT", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def fft_flops_per_row(info) -> float:
+    import math
+    L = info["fft_len"]
+    return 2 * 5.0 * L * math.log2(L) + 6.0 * L + 6.0 * (info["n_active"] + info["cols"])
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import numpy as np
+    import torch
+    import cuspfft_gb300 as gb
+    from cuspfft_gb300 import synthetic
+
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    dev = torch.cuda.current_device()
+    props = torch.cuda.get_device_properties(dev)
+    peaks = measured_peaks()
+
+    coo = synthetic.config_matrix(args.workload)
+    csc = gb.make_compact_csc(coo)
+    plan = gb.Plan(coo, length_policy=args.policy, u_tile=args.u_tile, csc=csc)
+    info = plan.info
+    out = plan.empty_output()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        plan.execute(out)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+
+    # ---- timed region: device time per step, phase times from the profiled entry
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    p1, p2 = [], []
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    for s in range(args.steps):
+        flush.fill_(s & 0xFF)
+        ev[s][0].record(stream)
+        a, b = plan.execute_profiled(out)
+        ev[s][1].record(stream)
+        p1.append(a)
+        p2.append(b)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    total_ms = sum(step_ms)
+    if pg:
+        t = torch.tensor([total_ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+        pg.barrier()
+    ffts = args.steps * world
+    ms_per_fft = total_ms / ffts
+    ms_per_step = total_ms / args.steps
+    n_tiles = (info["half_rows"] + info["u_tile"] - 1) // info["u_tile"]
+
+    # ---- roofline of each kernel
+    out_bytes = coo.rows * info["output_pitch"] * 8
+    s_bytes = info["half_rows"] * max(info["n_active"], 1) * 8
+    rows_bytes = out_bytes + s_bytes
+    rows_flops = info["half_rows"] * fft_flops_per_row(info)
+    p1_bytes = s_bytes + coo.nnz * info["index_bytes"] * ((info["half_rows"] + 127) // 128)
+    p1_flops = 2.0 * info["half_rows"] * coo.nnz
+    ms_p1 = statistics.mean(p1)
+    ms_rows = statistics.mean(p2)
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s nominal at max clock
+    kern = {
+        "k_bluestein_rows": {"ms": ms_rows, "bytes": rows_bytes, "flops": rows_flops},
+        "k_twiddle_sum": {"ms": ms_p1, "bytes": p1_bytes, "flops": p1_flops},
+    }
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    d = kern[dom]
+    achieved_gbs = d["bytes"] / (d["ms"] * 1e-3) / 1e9
+    achieved_tf = d["flops"] / (d["ms"] * 1e-3) / 1e12
+    traffic = None
+    tr_path = ROOT / "profiles" / "traffic.json"
+    if tr_path.exists():
+        try:
+            traffic = json.loads(tr_path.read_text()).get(args.workload, {}).get(dom)
+        except ValueError:
+            traffic = None
+    roofline = {
+        "kernel": dom, "bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+        "frac": round(achieved_gbs / hbm_peak, 4), "traffic": traffic,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+        "algorithmic_bytes_per_launch": d["bytes"] // n_tiles,
+        "fp32": {"achieved_tflops": round(achieved_tf, 2), "peak_tflops_nominal": round(fp32_peak, 1),
+                 "frac": round(achieved_tf / fp32_peak, 4)},
+        "kernels_ms": {k: round(v["ms"], 4) for k, v in kern.items()},
+    }
+
+    # ---- end to end through the reference-style API with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        pin_cp = torch.from_numpy(csc.col_ptr.copy()).pin_memory()
+        pin_ri = torch.from_numpy(csc.row_idx.copy()).pin_memory()
+        pin_sc = torch.from_numpy(csc.sparse_cols.copy()).pin_memory()
+        pin_csc = gb.CompactCSC(csc.n_sparse_cols, pin_sc.numpy(), pin_cp.numpy(), pin_ri.numpy())
+        host_out = torch.empty((coo.rows, info["output_pitch"]), dtype=torch.complex64).pin_memory()
+        times = []
+        for s in range(args.e2e_steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with gb.Plan(coo, length_policy=args.policy, u_tile=args.u_tile, csc=pin_csc) as p2plan:
+                o2 = p2plan.empty_output()
+                p2plan.execute(o2)
+                host_out.copy_(o2, non_blocking=True)
+                torch.cuda.synchronize()
+            del o2
+            if s > 0:
+                times.append((time.perf_counter() - t0) * 1e3)
+        h2d = int(pin_cp.numel() * 4 + coo.nnz * info["index_bytes"] + pin_sc.numel() * 4)
+        e2e = {"value": round(statistics.median(times), 4), "unit": "ms/FFT", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": int(out_bytes), "steps": len(times),
+               "includes": "plan build (CSC upload, FP64 tables), transform, D2H of the full spectrum"}
+
+    # ---- accuracy vs FP64 on sampled rows
+    acc = None
+    if not args.no_accuracy and rank == 0:
+        from oracle import fp64
+        g = np.random.default_rng(0)
+        us = np.unique(np.concatenate([[0, 1, coo.rows // 2, coo.rows - 1], g.integers(0, coo.rows, 28)]))
+        ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, us)
+        got = out[torch.as_tensor(us, device="cuda")].cpu().numpy()[:, : coo.cols // 2 + 1]
+        st = fp64.check_stats(got, ref)
+        acc = {"rel_l2_vs_fp64": st["rel_l2"], "max_abs": st["max_abs"], "rows_sampled": int(us.size)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(coo, args.cpu_budget)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(ms_per_fft, 4), "unit": "ms/FFT", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload],
+                       "shape": [coo.rows, coo.cols], "nnz": coo.nnz,
+                       "method": "sparse_fft_csc_bluestein_cufft_smooth" if args.policy == 7
+                       else "sparse_fft_csc_bluestein_mixed_radix",
+                       "fft_len": info["fft_len"], "channels": info["channels"], "radix": info["radix"],
+                       "u_tile": info["u_tile"], "l2": "flushed (512 MiB write) before each timed step",
+                       "parallelism": f"{world} independent replica(s)"},
+            "output_gbs": round(out_bytes / (ms_per_step * 1e-3) / 1e9, 1),
+            "gpu_launches": 2 * n_tiles * args.steps,
+            "clocks": clk, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "accuracy": acc,
+        }
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

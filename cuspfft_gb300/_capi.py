@@ -27,7 +27,7 @@ GBSP_LEN_7SMOOTH = 7
 EXPORTED = (
     "gbsp_version", "gbsp_status_string", "gbsp_last_error", "gbsp_read_mtx", "gbsp_free",
     "gbsp_build_compact_csc", "gbsp_next_smooth", "gbsp_plan_create", "gbsp_plan_get_info",
-    "gbsp_plan_destroy", "gbsp_execute", "gbsp_column_sums",
+    "gbsp_plan_destroy", "gbsp_execute", "gbsp_execute_profiled", "gbsp_column_sums",
 )
 
 
@@ -93,6 +93,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbsp_plan_get_info.argtypes = [vp, C.POINTER(GbspPlanInfo)]
     lib.gbsp_plan_destroy.argtypes = [vp]
     lib.gbsp_execute.argtypes = [vp, vp, C.c_size_t, vp]
+    lib.gbsp_execute_profiled.argtypes = [vp, vp, C.c_size_t, vp, C.POINTER(C.c_float),
+                                           C.POINTER(C.c_float)]
     lib.gbsp_column_sums.argtypes = [vp, i32, i32, vp, C.c_size_t, vp]
     for name in EXPORTED:
         if name not in ("gbsp_status_string", "gbsp_free"):

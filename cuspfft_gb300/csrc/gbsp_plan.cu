@@ -446,6 +446,50 @@ int gbsp_execute(gbsp_plan_t p, void* d_out, size_t out_pitch, void* stream) {
     return GBSP_OK;
 }
 
+int gbsp_execute_profiled(gbsp_plan_t p, void* d_out, size_t out_pitch, void* stream,
+                          float* ms_pass1, float* ms_rows) {
+    if (!p || !d_out || !ms_pass1 || !ms_rows)
+        return set_error(GBSP_ERR_INVALID, "gbsp_execute_profiled: null argument");
+    if (out_pitch < (size_t)p->out_cols || (out_pitch & 1) || ((uintptr_t)d_out & 15) != 0)
+        return set_error(GBSP_ERR_INVALID, "gbsp_execute_profiled: bad output pitch or alignment");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int ntiles = (p->half_rows + p->u_tile - 1) / p->u_tile;
+    std::vector<cudaEvent_t> ev(2 * ntiles + 1, nullptr);
+    int rc = GBSP_OK;
+    for (auto& e : ev) {
+        if (cudaEventCreate(&e) != cudaSuccess) { e = nullptr; rc = GBSP_ERR_CUDA; }
+    }
+    float a = 0.f, b = 0.f;
+    if (rc == GBSP_OK && cudaEventRecord(ev[0], st) != cudaSuccess) rc = GBSP_ERR_CUDA;
+    for (int t = 0; t < ntiles && rc == GBSP_OK; t++) {
+        const int u0 = t * p->u_tile;
+        const int n = std::min(p->u_tile, p->half_rows - u0);
+        pass1_dispatch(p, 2, u0, n, p->d_S, p->s_pitch, st);
+        if (cudaGetLastError() != cudaSuccess || cudaEventRecord(ev[2 * t + 1], st) != cudaSuccess) {
+            rc = GBSP_ERR_CUDA;
+            break;
+        }
+        rc = launch_rows(p, u0, n, d_out, out_pitch, st);
+        if (rc == GBSP_OK && (cudaGetLastError() != cudaSuccess ||
+                              cudaEventRecord(ev[2 * t + 2], st) != cudaSuccess))
+            rc = GBSP_ERR_CUDA;
+    }
+    if (rc == GBSP_OK && cudaEventSynchronize(ev[2 * ntiles]) != cudaSuccess) rc = GBSP_ERR_CUDA;
+    for (int t = 0; t < ntiles && rc == GBSP_OK; t++) {
+        float x = 0.f, y = 0.f;
+        cudaEventElapsedTime(&x, ev[2 * t], ev[2 * t + 1]);
+        cudaEventElapsedTime(&y, ev[2 * t + 1], ev[2 * t + 2]);
+        a += x;
+        b += y;
+    }
+    for (auto e : ev)
+        if (e) cudaEventDestroy(e);
+    if (rc != GBSP_OK) return set_error(rc, "gbsp_execute_profiled: CUDA failure");
+    *ms_pass1 = a;
+    *ms_rows = b;
+    return GBSP_OK;
+}
+
 int gbsp_column_sums(gbsp_plan_t p, int u0, int n_rows, void* d_s, size_t s_pitch, void* stream) {
     if (!p || !d_s) return set_error(GBSP_ERR_INVALID, "gbsp_column_sums: null argument");
     if (u0 < 0 || n_rows < 1 || u0 + n_rows > p->rows ||

@@ -144,6 +144,14 @@ class Plan:
         check(self._lib.gbsp_execute(self._h, C.c_void_p(out.data_ptr()), out.shape[1],
                                      _stream_handle(stream)), "gbsp_execute")
 
+    def execute_profiled(self, out, stream=None) -> tuple[float, float]:
+        """Runs execute() with events around each phase; returns (ms pass 1, ms rows)."""
+        a, b = C.c_float(), C.c_float()
+        check(self._lib.gbsp_execute_profiled(self._h, C.c_void_p(out.data_ptr()), out.shape[1],
+                                              _stream_handle(stream), C.byref(a), C.byref(b)),
+              "gbsp_execute_profiled")
+        return a.value, b.value
+
     def column_sums(self, u0: int, n_rows: int, out, stream=None) -> None:
         check(self._lib.gbsp_column_sums(self._h, u0, n_rows, C.c_void_p(out.data_ptr()), out.shape[1],
                                          _stream_handle(stream)), "gbsp_column_sums")

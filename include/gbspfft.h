@@ -128,6 +128,14 @@ int gbsp_plan_destroy(gbsp_plan_t plan);
  * on `stream`. */
 int gbsp_execute(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream);
 
+/* Same work as gbsp_execute, with CUDA events recorded around each phase on
+ * `stream`; blocks until the transform is done and returns the device time
+ * of each phase summed over tiles (milliseconds).  This is the reference's
+ * CUSPFFT_BREAKDOWN per-phase timing (src/sparse_fft_bluestein.cu:1752-1760,
+ * 1844-1950), exposed for every method. */
+int gbsp_execute_profiled(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream,
+                          float* ms_pass1, float* ms_rows);
+
 /* The pass-1 intermediate for inspection and tests: for Bluestein rows
  * [u0, u0+n_rows) writes S[u][j] = sum_{r in column j} exp(-2*pi*i*u*r/rows)
  * to d_s (complex64, row pitch s_pitch >= n_active).  n_rows <= the plan's
