@@ -166,13 +166,21 @@ template <bool INV, typename V> struct SmallDFT<8, INV, V> {
     }
 };
 
-// One stage of the FFT network on a buffer (shared or global memory).
+// Shared-memory index with one pad slot per 16 complex values: strides that
+// are multiples of 16 (power-of-two radices) no longer land on one bank.
+__device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded_len(int n) { return n + (n >> 4) + 1; }
+
+// One stage of the FFT network on a shared-memory buffer (padded indices).
 //   MODE 0: forward DIF stage
 //   MODE 1: inverse DIT stage
 //   MODE 2: last forward stage + pointwise filter multiply + first inverse
 //           stage (their twiddles cancel, so neither is applied)
-// Twiddle table layout for the stage: tw[k*(R-1) + (q-1)] = W_{R*m}^{q*k}.
-// `magic` = ceil(2^32 / m) gives j = t / m exactly for t, m < 2^16.
+// Twiddles are stored q-major per stage, tw[(q-1)*m + k] = W_{R*m}^{q*k}, so a
+// warp's loads for one q are contiguous.  The filter of the fused stage (the
+// last stage, m = 1, base = t*R) is stored in the same thread order,
+// filt[q*(Lp/R) + t].  `magic` = ceil(2^32/m) gives j = t/m exactly for
+// t, m < 2^16.
 template <int R, int MODE, typename V>
 __device__ __forceinline__ void fft_stage(V* __restrict__ buf, int Lp, int m, uint32_t magic,
                                           const V* __restrict__ tw, const V* __restrict__ filt,
@@ -185,29 +193,27 @@ __device__ __forceinline__ void fft_stage(V* __restrict__ buf, int Lp, int m, ui
         const int base = j * R * m + k;
         V a[R];
 #pragma unroll
-        for (int s = 0; s < R; s++) a[s] = buf[base + s * m];
+        for (int s = 0; s < R; s++) a[s] = buf[pad16(base + s * m)];
         if (MODE == 0) {
             SmallDFT<R, false, V>::run(a);
             if (k != 0) {
-                const V* w = tw + (size_t)k * (R - 1);
 #pragma unroll
-                for (int q = 1; q < R; q++) a[q] = cmul(a[q], w[q - 1]);
+                for (int q = 1; q < R; q++) a[q] = cmul(a[q], tw[(q - 1) * m + k]);
             }
         } else if (MODE == 1) {
             if (k != 0) {
-                const V* w = tw + (size_t)k * (R - 1);
 #pragma unroll
-                for (int q = 1; q < R; q++) a[q] = cmulc(a[q], w[q - 1]);
+                for (int q = 1; q < R; q++) a[q] = cmulc(a[q], tw[(q - 1) * m + k]);
             }
             SmallDFT<R, true, V>::run(a);
         } else {
             SmallDFT<R, false, V>::run(a);
 #pragma unroll
-            for (int q = 0; q < R; q++) a[q] = cmul(a[q], filt[base + q * m]);
+            for (int q = 0; q < R; q++) a[q] = cmul(a[q], filt[q * nb + t]);
             SmallDFT<R, true, V>::run(a);
         }
 #pragma unroll
-        for (int s = 0; s < R; s++) buf[base + s * m] = a[s];
+        for (int s = 0; s < R; s++) buf[pad16(base + s * m)] = a[s];
     }
 }
 

@@ -17,30 +17,43 @@ namespace gbsp {
 constexpr int MAX_STAGES = 16;
 constexpr int MAX_CHANNELS = 8;
 constexpr int ROWS_THREADS = 1024;  // k_bluestein_rows block size
-constexpr int PASS1_KU = 4;         // Bluestein rows per lane in k_twiddle_sum
-constexpr int PASS1_UBLK = 32 * PASS1_KU;
+constexpr int P1_THREADS = 512;     // k_twiddle_sum block size
+constexpr int P1_WARPS = P1_THREADS / 32;
+constexpr int P1_KU = 8;            // Bluestein rows per lane in k_twiddle_sum
+constexpr int P1_UBLK = 32 * P1_KU; // Bluestein rows per work item
+constexpr int P1_RESEED = 4;        // exact table lookup every P1_RESEED rows
+constexpr int P1_STAGE_PITCH = P1_WARPS + 1;
+constexpr size_t P1_STAGE_BYTES = (size_t)P1_UBLK * P1_STAGE_PITCH * 8;
 
 struct FFTDesc {
-    int Lp;
-    int nst;
-    int R[MAX_STAGES];
-    int m[MAX_STAGES];
-    uint32_t magic[MAX_STAGES];
-    int twoff[MAX_STAGES];
+    int Lp;                     // channel FFT length
+    int nst;                    // stages
+    int R[MAX_STAGES];          // radix per stage
+    int m[MAX_STAGES];          // span per stage
+    uint32_t magic[MAX_STAGES]; // ceil(2^32 / m)
+    int twoff[MAX_STAGES];      // stage twiddle offset in the global table (q-major blocks)
+    int rest_base;              // first twiddle of stage 1 (stages >= 1 are staged in smem)
+    int rest_len;               // twiddles of stages >= 1
 };
 
 // ---------------------------------------------------------------------------
 // Exact integer phase helpers
 // ---------------------------------------------------------------------------
 
-// x mod n for x < n^2 (so the true quotient is < n <= 65536): a float
-// estimate of the quotient is off by at most one, corrected both ways.
-__device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t n, float inv_n) {
-    uint32_t q = __float2uint_rz(__uint2float_rz(x) * inv_n);
-    int32_t r = (int32_t)(x - q * n);
-    r += (r < 0) ? (int32_t)n : 0;
-    r -= (r >= (int32_t)n) ? (int32_t)n : 0;
-    return (uint32_t)r;
+// x mod n for any 32-bit x and 2 <= n < 2^31 with magic = ceil(2^32 / n):
+// umulhi(x, magic) is floor(x/n) or floor(x/n)+1, corrected by one add.
+// (n == 1 uses magic 0 and only ever sees x == 0.)
+__device__ __forceinline__ uint32_t mod_magic(uint32_t x, uint32_t n, uint32_t magic) {
+    uint32_t q = __umulhi(x, magic);
+    uint32_t r = x - q * n;
+    return ((int32_t)r < 0) ? r + n : r;
+}
+
+// (u*r) mod rows; BIG handles rows > 65535 where u*r may not fit 32 bits.
+template <bool BIG>
+__device__ __forceinline__ uint32_t mulmod_rows(uint32_t u, uint32_t r, uint32_t rows, uint32_t magic) {
+    if (BIG) return (uint32_t)(((uint64_t)u * (uint64_t)r) % (uint64_t)rows);
+    return mod_magic(u * r, rows, magic);
 }
 
 // ---------------------------------------------------------------------------
@@ -57,32 +70,42 @@ __global__ void k_table_rows(float2* __restrict__ tab, int ntab, int rows) {
     tab[p] = make_float2((float)c, (float)s);
 }
 
-// pre[q][c]  = exp(-i*pi*c^2/cols) * W_L^{+c*q}   (chirp, channel pre-twiddle)
-// post[q][c] = exp(-i*pi*c^2/cols) * W_L^{-c*q}   (chirp, channel recombination)
-// with W_L = exp(-2*pi*i/L).  The chirp phase uses c^2 mod 2*cols exactly.
-__global__ void k_table_chirp(float2* __restrict__ pre, float2* __restrict__ post,
-                              int cols, int L, int K) {
+// Chirp exp(-i*pi*c^2/cols) times W_L^{+c*q} (sign = +1) or W_L^{-c*q} (sign = -1),
+// W_L = exp(-2*pi*i/L); c^2 mod 2*cols and c*q mod L are reduced exactly.
+__device__ __forceinline__ float2 chirp_twiddle(long long c, int q, int cols, int L, int sign) {
+    long long c2 = (c * c) % (2LL * cols);
+    long long cq = (c * (long long)q) % (long long)L;
+    double a = -(double)c2 / (double)cols - sign * 2.0 * (double)cq / (double)L;
+    double s, co;
+    sincospi(a, &s, &co);
+    return make_float2((float)co, (float)s);
+}
+
+// pre[q][j]  = chirp(c_j) * W_L^{+c_j*q}, c_j = slot_col[j]  (slot order)
+__global__ void k_table_pre(float2* __restrict__ pre, const int* __restrict__ slot_col, int n_slots,
+                            int cols, int L, int K) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)K * n_slots) return;
+    int q = (int)(idx / n_slots);
+    int j = (int)(idx - (long)q * n_slots);
+    pre[idx] = chirp_twiddle(slot_col[j], q, cols, L, +1);
+}
+
+// post[q][c] = chirp(c) * W_L^{-c*q}  (column order)
+__global__ void k_table_post(float2* __restrict__ post, int cols, int L, int K) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)K * cols) return;
     int q = (int)(idx / cols);
     int c = (int)(idx - (long)q * cols);
-    long long c2 = ((long long)c * (long long)c) % (2LL * cols);
-    long long cq = ((long long)c * (long long)q) % (long long)L;
-    double a = -(double)c2 / (double)cols;          // chirp: angle = pi * a
-    double b = -2.0 * (double)cq / (double)L;       // W_L^{cq}: angle = pi * b
-    double s, co;
-    sincospi(a + b, &s, &co);
-    pre[idx] = make_float2((float)co, (float)s);
-    sincospi(a - b, &s, &co);
-    post[idx] = make_float2((float)co, (float)s);
+    post[idx] = chirp_twiddle(c, q, cols, L, -1);
 }
 
-// Stage twiddles tw[off + k*(R-1) + q-1] = W_{Lp}^{q*k*l}, l = Lp/(R*m).
+// Stage twiddles, q-major: tw[off + (q-1)*m + k] = W_{Lp}^{q*k*l}, l = Lp/(R*m).
 __global__ void k_table_fft(float2* __restrict__ tw, int Lp, int R, int m, int off) {
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= m * (R - 1)) return;
-    int k = idx / (R - 1);
-    int q = idx - k * (R - 1) + 1;
+    int q = idx / m + 1;
+    int k = idx - (q - 1) * m;
     long long l = Lp / (R * m);
     long long e = ((long long)q * k * l) % Lp;
     double s, c;
@@ -155,29 +178,41 @@ __global__ void k_dif_stage_f64(double2* __restrict__ data, int K, int Lp, int R
     }
 }
 
-// filt = (float)(spec * scale)
+// filt[ch][q*(Lp/R) + t] = (float)(spec[ch][t*R + q] * scale): the filter in the
+// thread order of the fused last stage (radix R, span 1).
 __global__ void k_table_filter_final(float2* __restrict__ filt, const double2* __restrict__ spec,
-                                     long n, double scale) {
+                                     int K, int Lp, int R, double scale) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n) return;
+    if (idx >= (long)K * Lp) return;
+    int ch = (int)(idx / Lp);
+    int pos = (int)(idx - (long)ch * Lp);
+    int t = pos / R, q = pos - (pos / R) * R;
     double2 v = spec[idx];
-    filt[idx] = make_float2((float)(v.x * scale), (float)(v.y * scale));
+    filt[(size_t)ch * Lp + (size_t)q * (Lp / R) + t] = make_float2((float)(v.x * scale), (float)(v.y * scale));
 }
 
 // ---------------------------------------------------------------------------
 // Pass 1: twiddle sums over each active column's nonzero rows.
 //
-// Work item = (block of PASS1_UBLK Bluestein rows, one active column) handled
-// by one warp; lane l owns rows u = ubase + l + 32*i (i < KU).  Per nonzero r
-// the lane computes its phase (u*r) mod rows once with exact integer
-// arithmetic and then steps it by (32*r) mod rows, so only one modular
-// multiply is spent per KU twiddles.  Twiddles come from a table staged in
-// shared memory: the whole circle (TAB_HALF = false) or the half circle
-// p <= rows/2 with W^{rows-p} = conj(W^p).  Columns with at least
-// kahan_min nonzeros accumulate with Kahan-compensated FP32 additions.
+// Columns live in "slots" sorted by degree (descending), so the P1_WARPS
+// columns of one work item have nearly equal nonzero counts.  A work item is
+// (block of P1_UBLK Bluestein rows, group of P1_WARPS slots); warp w owns
+// slot g*P1_WARPS + w and lane l owns rows u = ubase + l + 32*kk (kk < KU).
 //
-// The reference evaluates __sincosf of a float angle per (u, nonzero) and
-// does one output row per thread (src/sparse_fft_bluestein.cu:366-397).
+// Per nonzero r the lane reduces its phase (u*r) mod rows exactly with an
+// integer multiply-high and reads W_rows^p from the table staged in shared
+// memory.  The rows u + 32*kk in between reuse the exactly looked-up
+// W_rows^{(32*r) mod rows} as a complex multiplier, and every P1_RESEED rows
+// the value is looked up exactly again, so no twiddle is more than
+// P1_RESEED-1 products away from a correctly rounded table entry.  Sums of a
+// batch of 32 nonzeros are added to the column total; for columns with at
+// least kahan_min nonzeros that addition is Kahan-compensated.  Results pass
+// through a shared-memory tile so every S row segment is written as whole
+// 128-byte lines.
+//
+// The reference evaluates __sincosf of a float angle per (u, nonzero), one
+// output row per thread, and writes strided 8-byte values
+// (src/sparse_fft_bluestein.cu:366-397).
 // ---------------------------------------------------------------------------
 template <bool TAB_HALF>
 __device__ __forceinline__ float2 row_twiddle(const float2* tab, uint32_t p, uint32_t rows, uint32_t hr) {
@@ -188,93 +223,106 @@ __device__ __forceinline__ float2 row_twiddle(const float2* tab, uint32_t p, uin
     return w;
 }
 
-// (u*r) mod rows; BIG handles rows > 65536 where u*r no longer fits 32 bits.
-template <bool BIG>
-__device__ __forceinline__ uint32_t mulmod_rows(uint32_t u, uint32_t r, uint32_t rows, float inv_rows) {
-    if (BIG) return (uint32_t)(((uint64_t)u * (uint64_t)r) % (uint64_t)rows);
-    return mod_small(u * r, rows, inv_rows);
-}
-
-template <typename IDX, bool TAB_HALF, bool KAHAN, bool BIG>
-__device__ __forceinline__ void column_sum_loop(const IDX* __restrict__ row_idx, int beg, int end,
-                                                const float2* tab, uint32_t u_lane, uint32_t rows,
-                                                float inv_rows, int lane, float (&ax)[PASS1_KU],
-                                                float (&ay)[PASS1_KU]) {
-    float cx[PASS1_KU], cy[PASS1_KU];
+template <typename IDX, bool TAB_HALF, bool BIG>
+__device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx, int beg, int end,
+                                                 const float2* tab, uint32_t u_lane, uint32_t rows,
+                                                 uint32_t magic, int lane, bool compensated,
+                                                 float2 (&acc)[P1_KU]) {
+    float2 cmp[P1_KU];
 #pragma unroll
-    for (int i = 0; i < PASS1_KU; i++) { cx[i] = 0.f; cy[i] = 0.f; }
+    for (int i = 0; i < P1_KU; i++) { acc[i] = make_float2(0.f, 0.f); cmp[i] = make_float2(0.f, 0.f); }
     const uint32_t hr = rows / 2;
     for (int p0 = beg; p0 < end; p0 += 32) {
-        int cnt = min(32, end - p0);
-        uint32_t rl = 0, dl = 0;
+        const int cnt = min(32, end - p0);
+        uint32_t rl = 0, sl = 0;
+        float2 wl = make_float2(1.f, 0.f);
         if (lane < cnt) {
             rl = (uint32_t)row_idx[p0 + lane];
-            dl = mulmod_rows<BIG>(32u, rl, rows, inv_rows);
+            const uint32_t d = mulmod_rows<BIG>(32u, rl, rows, magic);
+            wl = row_twiddle<TAB_HALF>(tab, d, rows, hr);
+            sl = mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic);
         }
-        for (int i = 0; i < cnt; i++) {
-            uint32_t r = __shfl_sync(0xffffffffu, rl, i);
-            uint32_t d = __shfl_sync(0xffffffffu, dl, i);
-            uint32_t p = mulmod_rows<BIG>(u_lane, r, rows, inv_rows);
+        float2 blk[P1_KU];
 #pragma unroll
-            for (int kk = 0; kk < PASS1_KU; kk++) {
-                float2 w = row_twiddle<TAB_HALF>(tab, p, rows, hr);
-                if (KAHAN) {
-                    float y = w.x - cx[kk];
-                    float t = ax[kk] + y;
-                    cx[kk] = (t - ax[kk]) - y;
-                    ax[kk] = t;
-                    y = w.y - cy[kk];
-                    t = ay[kk] + y;
-                    cy[kk] = (t - ay[kk]) - y;
-                    ay[kk] = t;
+        for (int i = 0; i < P1_KU; i++) blk[i] = make_float2(0.f, 0.f);
+        for (int i = 0; i < cnt; i++) {
+            const uint32_t r = __shfl_sync(0xffffffffu, rl, i);
+            const uint32_t step = __shfl_sync(0xffffffffu, sl, i);
+            const float2 wd = make_float2(__shfl_sync(0xffffffffu, wl.x, i),
+                                          __shfl_sync(0xffffffffu, wl.y, i));
+            uint32_t p = mulmod_rows<BIG>(u_lane, r, rows, magic);
+            float2 w = make_float2(1.f, 0.f);
+#pragma unroll
+            for (int kk = 0; kk < P1_KU; kk++) {
+                if (kk % P1_RESEED == 0) {
+                    w = row_twiddle<TAB_HALF>(tab, p, rows, hr);
+                    const uint32_t pn = p + step;
+                    p = min(pn, pn - rows);
                 } else {
-                    ax[kk] += w.x;
-                    ay[kk] += w.y;
+                    w = cmul(w, wd);
                 }
-                uint32_t pn = p + d;
-                p = min(pn, pn - rows);
+                blk[kk].x += w.x;
+                blk[kk].y += w.y;
             }
+        }
+        if (compensated) {
+#pragma unroll
+            for (int kk = 0; kk < P1_KU; kk++) {
+                float y = blk[kk].x - cmp[kk].x;
+                float t = acc[kk].x + y;
+                cmp[kk].x = (t - acc[kk].x) - y;
+                acc[kk].x = t;
+                y = blk[kk].y - cmp[kk].y;
+                t = acc[kk].y + y;
+                cmp[kk].y = (t - acc[kk].y) - y;
+                acc[kk].y = t;
+            }
+        } else {
+#pragma unroll
+            for (int kk = 0; kk < P1_KU; kk++) { acc[kk].x += blk[kk].x; acc[kk].y += blk[kk].y; }
         }
     }
 }
 
 template <typename IDX, bool TAB_HALF, bool BIG>
-__global__ void __launch_bounds__(512)
-k_twiddle_sum(const int* __restrict__ col_ptr, const IDX* __restrict__ row_idx, int n_active,
-              const float2* __restrict__ row_tab, int ntab, int rows, float inv_rows,
+__global__ void __launch_bounds__(P1_THREADS)
+k_twiddle_sum(const int* __restrict__ slot_ptr, const IDX* __restrict__ row_idx, int n_slots,
+              const float2* __restrict__ row_tab, int ntab, int rows, uint32_t magic,
               int u0, int tile_rows, float2* __restrict__ S, size_t s_pitch, int kahan_min) {
     extern __shared__ float4 smem_raw[];
-    float2* tab = reinterpret_cast<float2*>(smem_raw);
+    float2* stage = reinterpret_cast<float2*>(smem_raw);
+    float2* tab = stage + P1_UBLK * P1_STAGE_PITCH;
     for (int i = threadIdx.x; i < ntab; i += blockDim.x) tab[i] = row_tab[i];
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    const long gw = (long)blockIdx.x * wpb + (threadIdx.x >> 5);
-    const long nw = (long)gridDim.x * wpb;
-    const int n_ublk = (tile_rows + PASS1_UBLK - 1) / PASS1_UBLK;
-    const long nitems = (long)n_ublk * n_active;
+    const int warp = threadIdx.x >> 5;
+    const int n_ublk = (tile_rows + P1_UBLK - 1) / P1_UBLK;
+    const int n_grp = (n_slots + P1_WARPS - 1) / P1_WARPS;
+    const long nitems = (long)n_ublk * n_grp;
 
-    for (long it = gw; it < nitems; it += nw) {
-        const int ub = (int)(it / n_active);
-        const int j = (int)(it - (long)ub * n_active);
-        const int ul0 = ub * PASS1_UBLK;
-        uint32_t u_lane = (uint32_t)(u0 + ul0 + lane) % (uint32_t)rows;
-        const int beg = col_ptr[j], end = col_ptr[j + 1];
-        float ax[PASS1_KU], ay[PASS1_KU];
+    for (long it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int ub = (int)(it / n_grp);
+        const int g = (int)(it - (long)ub * n_grp);
+        const int ul0 = ub * P1_UBLK;
+        const int j = g * P1_WARPS + warp;
+        if (j < n_slots) {
+            const uint32_t u_lane = (uint32_t)(u0 + ul0 + lane) % (uint32_t)rows;
+            const int beg = slot_ptr[j], end = slot_ptr[j + 1];
+            float2 acc[P1_KU];
+            column_sums_warp<IDX, TAB_HALF, BIG>(row_idx, beg, end, tab, u_lane, (uint32_t)rows, magic,
+                                                 lane, kahan_min > 0 && end - beg >= kahan_min, acc);
 #pragma unroll
-        for (int i = 0; i < PASS1_KU; i++) { ax[i] = 0.f; ay[i] = 0.f; }
-        if (kahan_min > 0 && end - beg >= kahan_min)
-            column_sum_loop<IDX, TAB_HALF, true, BIG>(row_idx, beg, end, tab, u_lane, (uint32_t)rows,
-                                                 inv_rows, lane, ax, ay);
-        else
-            column_sum_loop<IDX, TAB_HALF, false, BIG>(row_idx, beg, end, tab, u_lane, (uint32_t)rows,
-                                                  inv_rows, lane, ax, ay);
-#pragma unroll
-        for (int kk = 0; kk < PASS1_KU; kk++) {
-            int ul = ul0 + lane + 32 * kk;
-            if (ul < tile_rows) S[(size_t)ul * s_pitch + j] = make_float2(ax[kk], ay[kk]);
+            for (int kk = 0; kk < P1_KU; kk++) stage[(lane + 32 * kk) * P1_STAGE_PITCH + warp] = acc[kk];
         }
+        __syncthreads();
+        for (int e = threadIdx.x; e < P1_UBLK * P1_WARPS; e += blockDim.x) {
+            const int row = e / P1_WARPS, col = e - (e / P1_WARPS) * P1_WARPS;
+            const int ul = ul0 + row, jj = g * P1_WARPS + col;
+            if (ul < tile_rows && jj < n_slots)
+                S[(size_t)ul * s_pitch + jj] = stage[row * P1_STAGE_PITCH + col];
+        }
+        __syncthreads();
     }
 }
 
@@ -290,21 +338,27 @@ k_twiddle_sum(const int* __restrict__ col_ptr, const IDX* __restrict__ row_idx, 
 // (u <= rows/2) writes output rows u and rows-u, each with 16-byte stores of
 // two complex values.
 //
+// Shared memory: the padded row buffer, then the twiddles of stages >= 1
+// (loaded once per CTA); stage 0's twiddles stream from L2.
+//
 // The reference runs 2F+4 launches per tile of rows with a global round trip
 // per stage (src/sparse_fft_bluestein.cu:2327-2370) and writes 8-byte stores
 // in bluestein_finalize_kernel (:469-486).
 // ---------------------------------------------------------------------------
 template <bool CLUSTER>
 __global__ void __launch_bounds__(ROWS_THREADS, 1)
-k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_active,
-                 const int* __restrict__ sparse_cols, const float2* __restrict__ pre,
+k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_slots,
+                 const int* __restrict__ slot_col, const float2* __restrict__ pre,
                  const float2* __restrict__ post, const float2* __restrict__ filt,
                  const float2* __restrict__ fft_tw, FFTDesc fd, int K, int rows, int cols,
                  int u0, int tile_rows, float2* __restrict__ out, size_t out_pitch) {
     extern __shared__ float4 smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);
     const int Lp = fd.Lp;
+    const int Lpad = padded_len(Lp);
+    float2* twr = buf + Lpad;
     const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < fd.rest_len; i += nt) twr[i] = fft_tw[fd.rest_base + i];
 
     int q = 0, cid = blockIdx.x, ncl = gridDim.x;
     const float2* zsrc[MAX_CHANNELS];
@@ -319,30 +373,37 @@ k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_active,
     } else {
         zsrc[0] = buf;
     }
-    const float2* preq = pre + (size_t)q * cols;
+    const float2* preq = pre + (size_t)q * n_slots;
     const float2* filtq = filt + (size_t)q * Lp;
     const int half_slots = (int)(out_pitch >> 1);
     const int hc = cols / 2;
     const bool wrap_in = cols > Lp;
+    // stage 0 twiddles stream from global memory, the rest sit in shared memory
+    auto tw_of = [&](int s) -> const float2* {
+        return (s == 0) ? fft_tw + fd.twoff[0] : twr + (fd.twoff[s] - fd.rest_base);
+    };
 
     for (int t = cid; t < tile_rows; t += ncl) {
         const int u = u0 + t;
-        for (int i = tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
+        for (int i = tid; i < Lpad; i += nt) buf[i] = make_float2(0.f, 0.f);
         __syncthreads();
         const float2* srow = S + (size_t)t * s_pitch;
         if (!wrap_in) {
-            for (int j = tid; j < n_active; j += nt) {
-                int c = sparse_cols[j];
-                buf[c] = cmul(srow[j], preq[c]);
+            for (int j = tid; j < n_slots; j += nt) {
+                const int c = slot_col[j];
+                buf[pad16(c)] = cmul(srow[j], preq[j]);
             }
             __syncthreads();
         } else {
             // several input columns fold onto one slot: add section by section
             for (int sec = 0; sec * Lp < cols; sec++) {
                 const int lo = sec * Lp, hi = lo + Lp;
-                for (int j = tid; j < n_active; j += nt) {
-                    int c = sparse_cols[j];
-                    if (c >= lo && c < hi) buf[c - lo] = cadd(buf[c - lo], cmul(srow[j], preq[c]));
+                for (int j = tid; j < n_slots; j += nt) {
+                    const int c = slot_col[j];
+                    if (c >= lo && c < hi) {
+                        float2* d = buf + pad16(c - lo);
+                        *d = cadd(*d, cmul(srow[j], preq[j]));
+                    }
                 }
                 __syncthreads();
             }
@@ -350,15 +411,14 @@ k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_active,
         // forward DIF, filter multiply fused with the last stage, inverse DIT
         const int S1 = fd.nst - 1;
         for (int s = 0; s < S1; s++) {
-            fft_stage_dispatch<0>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], fft_tw + fd.twoff[s],
+            fft_stage_dispatch<0>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
                                   (const float2*)nullptr, tid, nt);
             __syncthreads();
         }
-        fft_stage_dispatch<2>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], fft_tw + fd.twoff[S1],
-                              filtq, tid, nt);
+        fft_stage_dispatch<2>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
         __syncthreads();
         for (int s = S1 - 1; s >= 0; s--) {
-            fft_stage_dispatch<1>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], fft_tw + fd.twoff[s],
+            fft_stage_dispatch<1>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
                                   (const float2*)nullptr, tid, nt);
             __syncthreads();
         }
@@ -378,14 +438,15 @@ k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_active,
                 const int vv = v + e;
                 float2 val = make_float2(0.f, 0.f);
                 if (vv <= hc) {
-                    int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
+                    const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
                     int n = c;
                     while (n >= Lp) n -= Lp;
+                    const int pn = pad16(n);
                     if (CLUSTER) {
                         for (int qq = 0; qq < K; qq++)
-                            val = cadd(val, cmul(zsrc[qq][n], post[(size_t)qq * cols + c]));
+                            val = cadd(val, cmul(zsrc[qq][pn], post[(size_t)qq * cols + c]));
                     } else {
-                        val = cmul(buf[n], post[c]);
+                        val = cmul(buf[pn], post[c]);
                     }
                     if (sel) val.y = -val.y;
                 }

@@ -58,7 +58,7 @@ typedef struct {
     int max_channel_len;   /* largest per-CTA FFT length held in shared memory;
                               0 = default; longer convolutions split into channels that
                               run as one thread-block cluster                             */
-    int pass1_threads;     /* 0 = default (512)                                          */
+    int reserved0;         /* must be 0                                                  */
     int reserved[8];
 } gbsp_options;
 
@@ -136,13 +136,19 @@ int gbsp_execute(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream);
 int gbsp_execute_profiled(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream,
                           float* ms_pass1, float* ms_rows);
 
-/* The pass-1 intermediate for inspection and tests: for Bluestein rows
- * [u0, u0+n_rows) writes S[u][j] = sum_{r in column j} exp(-2*pi*i*u*r/rows)
- * to d_s (complex64, row pitch s_pitch >= n_active).  n_rows <= the plan's
- * u_tile.  This is the reference's csc_build_bluestein_input_*kernel
- * (src/sparse_fft_bluestein.cu:334-397) before its chirp multiply. */
+/* The pass-1 intermediate for inspection and tests: for rows
+ * u in [u0, u0+n_rows) (u0+n_rows <= rows) writes
+ *   S[u-u0][j] = sum over nonzero rows r of slot j of exp(-2*pi*i*u*r/rows)
+ * to d_s (complex64, row pitch s_pitch >= n_active).  Slots are the active
+ * columns ordered by decreasing nonzero count; gbsp_plan_slot_columns gives
+ * the column of each slot.  This is the reference's
+ * csc_build_bluestein_input_*kernel (src/sparse_fft_bluestein.cu:334-397)
+ * before its chirp multiply. */
 int gbsp_column_sums(gbsp_plan_t plan, int u0, int n_rows, void* d_s, size_t s_pitch,
                      void* stream);
+
+/* Copies the column index of each slot (n_active ints) to host memory. */
+int gbsp_plan_slot_columns(gbsp_plan_t plan, int* cols_out);
 
 #ifdef __cplusplus
 }

@@ -73,7 +73,7 @@ def test_u_tiles_and_index_width(cuda):
     coo = synthetic.uniform_matrix(257, 300, 4000, seed=9)
     base, _ = run_plan(coo)
     for kw in ({"u_tile": 1}, {"u_tile": 5}, {"u_tile": 64}, {"index_bytes": 4},
-               {"kahan_min_degree": 1}, {"kahan_min_degree": -1}, {"pass1_threads": 64}):
+               {"kahan_min_degree": 1}, {"kahan_min_degree": -1}):
         got, _ = run_plan(coo, **kw)
         check_against_oracle(coo, got)
         assert fp64.rel_l2(got, base) < 1e-5
@@ -126,12 +126,16 @@ def test_column_sums(cuda):
     coo = synthetic.uniform_matrix(211, 77, 2000, seed=5)
     csc = gb.make_compact_csc(coo)
     with gb.Plan(coo) as plan:
-        s = torch.zeros((20, csc.n_sparse_cols), dtype=torch.complex64, device="cuda")
-        plan.column_sums(30, 20, s)
+        slots = plan.slot_columns()
+        s = torch.zeros((150, csc.n_sparse_cols), dtype=torch.complex64, device="cuda")
+        plan.column_sums(30, 150, s)
         torch.cuda.synchronize()
         got = s.cpu().numpy()
-    ref = fp64.column_sums_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, np.arange(30, 50))
-    assert fp64.rel_l2(got, ref[:, csc.sparse_cols]) < 1e-6
+    assert sorted(slots.tolist()) == csc.sparse_cols.tolist()
+    deg = np.diff(csc.col_ptr)[np.searchsorted(csc.sparse_cols, slots)]
+    assert np.all(np.diff(deg) <= 0), "slots must be ordered by decreasing degree"
+    ref = fp64.column_sums_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, np.arange(30, 180))
+    assert fp64.rel_l2(got, ref[:, slots]) < 1e-6
 
 
 def test_config_uniform_3001x2048_full(cuda):
