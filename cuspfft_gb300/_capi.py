@@ -28,7 +28,7 @@ EXPORTED = (
     "gbsp_version", "gbsp_status_string", "gbsp_last_error", "gbsp_read_mtx", "gbsp_free",
     "gbsp_build_compact_csc", "gbsp_next_smooth", "gbsp_plan_create", "gbsp_plan_get_info",
     "gbsp_plan_destroy", "gbsp_execute", "gbsp_execute_profiled", "gbsp_column_sums",
-    "gbsp_plan_slot_columns",
+    "gbsp_plan_error_flags",
 )
 
 
@@ -39,8 +39,10 @@ class GbspOptions(C.Structure):
         ("kahan_min_degree", C.c_int),
         ("index_bytes", C.c_int),
         ("max_channel_len", C.c_int),
-        ("reserved0", C.c_int),
-        ("reserved", C.c_int * 8),
+        ("rows_threads", C.c_int),
+        ("row_table_mode", C.c_int),
+        ("radix", C.c_int * 8),
+        ("reserved", C.c_int * 4),
     ]
 
 
@@ -50,7 +52,8 @@ class GbspPlanInfo(C.Structure):
         ("fft_len", C.c_int), ("channels", C.c_int), ("channel_len", C.c_int),
         ("n_stages", C.c_int), ("radix", C.c_int * 16), ("output_cols", C.c_int),
         ("output_pitch", C.c_int), ("half_rows", C.c_int), ("u_tile", C.c_int),
-        ("index_bytes", C.c_int), ("row_table_mode", C.c_int), ("device_bytes", C.c_size_t),
+        ("index_bytes", C.c_int), ("row_table_mode", C.c_int), ("rows_threads", C.c_int),
+        ("device_bytes", C.c_size_t),
     ]
 
     def as_dict(self) -> dict:
@@ -97,7 +100,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbsp_execute_profiled.argtypes = [vp, vp, C.c_size_t, vp, C.POINTER(C.c_float),
                                            C.POINTER(C.c_float)]
     lib.gbsp_column_sums.argtypes = [vp, i32, i32, vp, C.c_size_t, vp]
-    lib.gbsp_plan_slot_columns.argtypes = [vp, ip]
+    lib.gbsp_plan_error_flags.argtypes = [vp, ip]
     for name in EXPORTED:
         if name not in ("gbsp_status_string", "gbsp_free"):
             getattr(lib, name).restype = i32

@@ -18,6 +18,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+#include <utility>
+
 namespace gbsp {
 
 template <typename T> struct vec2;
@@ -166,12 +169,143 @@ template <bool INV, typename V> struct SmallDFT<8, INV, V> {
     }
 };
 
-// Shared-memory index with one pad slot per 16 complex values: strides that
-// are multiples of 16 (power-of-two radices) no longer land on one bank.
-__device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
-__host__ __device__ constexpr int padded_len(int n) { return n + (n >> 4) + 1; }
+// ---------------------------------------------------------------------------
+// Compile-time roots of unity for the composite radices: cos / sin of
+// 2*pi*j/n with the angle folded into [0, pi/4] by exact integer symmetry,
+// then a Taylor series in double (error far below float rounding).
+// ---------------------------------------------------------------------------
+struct Root { double c, s; };
 
-// One stage of the FFT network on a shared-memory buffer (padded indices).
+__host__ __device__ constexpr double ct_sin(double x) {
+    double t = x, acc = x;
+    for (int k = 1; k < 14; k++) { t *= -x * x / ((2.0 * k) * (2.0 * k + 1.0)); acc += t; }
+    return acc;
+}
+__host__ __device__ constexpr double ct_cos(double x) {
+    double t = 1.0, acc = 1.0;
+    for (int k = 1; k < 14; k++) { t *= -x * x / ((2.0 * k - 1.0) * (2.0 * k)); acc += t; }
+    return acc;
+}
+// angle 2*pi*j/n
+__host__ __device__ constexpr Root unit_root(long j, long n) {
+    j %= n;
+    if (j < 0) j += n;
+    if (2 * j > n) {  // (pi, 2pi): mirror
+        Root r = unit_root(n - j, n);
+        return Root{r.c, -r.s};
+    }
+    if (4 * j > n) {  // (pi/2, pi]: cos(t) = -cos(pi - t), sin(t) = sin(pi - t)
+        Root r = unit_root(n - 2 * j, 2 * n);
+        return Root{-r.c, r.s};
+    }
+    if (8 * j > n) {  // (pi/4, pi/2]: swap with pi/2 - t
+        Root r = unit_root(n - 4 * j, 4 * n);
+        return Root{r.s, r.c};
+    }
+    const double x = 6.283185307179586476925286766559 * (double)j / (double)n;
+    return Root{ct_cos(x), ct_sin(x)};
+}
+
+template <int N, typename F, int... I>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, I...>) {
+    (f(std::integral_constant<int, I>{}), ...);
+}
+// f(integral_constant<int, i>) for i = 0..N-1, each index a compile-time constant
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+    static_for_impl<N>(f, std::make_integer_sequence<int, N>{});
+}
+
+// x * W_P^{E} (forward, W_P = exp(-2*pi*i/P)) or x * W_P^{-E} (inverse)
+template <int P, int E, bool INV, typename V>
+__device__ __forceinline__ V mul_root(V x) {
+    constexpr int e = E % P;
+    if constexpr (e == 0) {
+        return x;
+    } else if constexpr (2 * e == P) {
+        return mk<V>(-x.x, -x.y);
+    } else if constexpr (4 * e == P) {
+        return mul_mi<INV>(x);
+    } else if constexpr (4 * e == 3 * P) {
+        return mul_mi<!INV>(x);
+    } else {
+        using T = decltype(V::x);
+        constexpr Root r = unit_root(e, P);
+        const T c = (T)r.c, sn = INV ? (T)r.s : (T)-r.s;
+        return mk<V>(fma(x.x, c, -x.y * sn), fma(x.x, sn, x.y * c));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Radix<P>: the P-point DFT of one butterfly held in registers.
+//   fwd(a): a[] natural-order input -> outputs X[q] at register out_reg(q)
+//   inv(a): inputs X[q] at register out_reg(q) -> natural-order a[] (unscaled)
+// Prime-power radices 2..8 use SmallDFT (out_reg = identity).  A composite
+// P = A*B splits n = B*n1 + n2, q = k1 + A*k2: A-point DFTs over n1, the
+// twiddles W_P^{n2*k1}, then B-point DFTs over n2, leaving X[k1 + A*k2] in
+// register B*k1 + k2 -- no register shuffles, the stage's loads and stores
+// absorb the permutation.
+// ---------------------------------------------------------------------------
+template <int P> struct Split;  // composite radices: A * B
+template <> struct Split<9>  { static constexpr int A = 3, B = 3; };
+template <> struct Split<12> { static constexpr int A = 4, B = 3; };
+template <> struct Split<15> { static constexpr int A = 5, B = 3; };
+template <> struct Split<16> { static constexpr int A = 4, B = 4; };
+template <> struct Split<20> { static constexpr int A = 5, B = 4; };
+template <> struct Split<21> { static constexpr int A = 7, B = 3; };
+template <> struct Split<24> { static constexpr int A = 8, B = 3; };
+template <> struct Split<25> { static constexpr int A = 5, B = 5; };
+template <> struct Split<28> { static constexpr int A = 7, B = 4; };
+template <> struct Split<32> { static constexpr int A = 8, B = 4; };
+template <> struct Split<35> { static constexpr int A = 7, B = 5; };
+template <> struct Split<40> { static constexpr int A = 8, B = 5; };
+
+template <int P> struct IsBase { static constexpr bool value = (P == 2 || P == 3 || P == 4 || P == 5 || P == 7 || P == 8); };
+
+template <int P, bool BASE = IsBase<P>::value> struct Radix;
+
+template <int P> struct Radix<P, true> {
+    __host__ __device__ static constexpr int out_reg(int q) { return q; }
+    template <typename V> __device__ __forceinline__ static void fwd(V* a) { SmallDFT<P, false, V>::run(a); }
+    template <typename V> __device__ __forceinline__ static void inv(V* a) { SmallDFT<P, true, V>::run(a); }
+};
+
+template <int P> struct Radix<P, false> {
+    static constexpr int A = Split<P>::A, B = Split<P>::B;
+    __host__ __device__ static constexpr int out_reg(int q) { return B * (q % A) + q / A; }
+    template <typename V> __device__ __forceinline__ static void fwd(V* a) {
+        static_for<B>([&](auto n2c) {
+            constexpr int n2 = decltype(n2c)::value;
+            V x[A];
+#pragma unroll
+            for (int n1 = 0; n1 < A; n1++) x[n1] = a[B * n1 + n2];
+            SmallDFT<A, false, V>::run(x);
+            static_for<A>([&](auto k1c) {
+                constexpr int k1 = decltype(k1c)::value;
+                a[B * k1 + n2] = mul_root<P, n2 * k1, false>(x[k1]);
+            });
+        });
+#pragma unroll
+        for (int k1 = 0; k1 < A; k1++) SmallDFT<B, false, V>::run(a + B * k1);
+    }
+    template <typename V> __device__ __forceinline__ static void inv(V* a) {
+#pragma unroll
+        for (int k1 = 0; k1 < A; k1++) SmallDFT<B, true, V>::run(a + B * k1);
+        static_for<B>([&](auto n2c) {
+            constexpr int n2 = decltype(n2c)::value;
+            V x[A];
+            static_for<A>([&](auto k1c) {
+                constexpr int k1 = decltype(k1c)::value;
+                x[k1] = mul_root<P, n2 * k1, true>(a[B * k1 + n2]);
+            });
+            SmallDFT<A, true, V>::run(x);
+#pragma unroll
+            for (int n1 = 0; n1 < A; n1++) a[B * n1 + n2] = x[n1];
+        });
+    }
+};
+
+// One stage of the FFT network on a shared-memory buffer.
 //   MODE 0: forward DIF stage
 //   MODE 1: inverse DIT stage
 //   MODE 2: last forward stage + pointwise filter multiply + first inverse
@@ -179,54 +313,88 @@ __host__ __device__ constexpr int padded_len(int n) { return n + (n >> 4) + 1; }
 // Twiddles are stored q-major per stage, tw[(q-1)*m + k] = W_{R*m}^{q*k}, so a
 // warp's loads for one q are contiguous.  The filter of the fused stage (the
 // last stage, m = 1, base = t*R) is stored in the same thread order,
-// filt[q*(Lp/R) + t].  `magic` = ceil(2^32/m) gives j = t/m exactly for
-// t, m < 2^16.
+// filt[q*(Lp/R) + t].
+//
+// Thread -> butterfly mapping: for spans m >= 16 consecutive threads take
+// consecutive k (unit-stride shared-memory accesses); for shorter spans with
+// R*m odd they take consecutive j, i.e. stride R*m, which hits distinct banks.
+// `magic` = ceil(2^32/d) gives t/d exactly for t, d < 2^16 where d is m
+// (k-fastest) or l = Lp/(R*m) (j-fastest).
+__host__ __device__ constexpr bool stage_j_fastest(int R, int m, int l) {
+    return m > 1 && m < 16 && l > 1 && ((R * m) & 1) == 1;
+}
+
 template <int R, int MODE, typename V>
 __device__ __forceinline__ void fft_stage(V* __restrict__ buf, int Lp, int m, uint32_t magic,
                                           const V* __restrict__ tw, const V* __restrict__ filt,
                                           int tid, int nthreads) {
+    using RX = Radix<R>;
     const int nb = Lp / R;
+    const int l = nb / m;
+    const bool jfast = stage_j_fastest(R, m, l);
     for (int t = tid; t < nb; t += nthreads) {
         int j, k;
         if (m == 1) { j = t; k = 0; }
-        else { j = (int)__umulhi((uint32_t)t, magic); k = t - j * m; }
+        else if (!jfast) { j = (int)__umulhi((uint32_t)t, magic); k = t - j * m; }
+        else { k = (int)__umulhi((uint32_t)t, magic); j = t - k * l; }
         const int base = j * R * m + k;
         V a[R];
+        if (MODE == 1) {
+            // inputs q sit in register out_reg(q)
 #pragma unroll
-        for (int s = 0; s < R; s++) a[s] = buf[pad16(base + s * m)];
-        if (MODE == 0) {
-            SmallDFT<R, false, V>::run(a);
+            for (int q = 0; q < R; q++) a[RX::out_reg(q)] = buf[base + q * m];
             if (k != 0) {
 #pragma unroll
-                for (int q = 1; q < R; q++) a[q] = cmul(a[q], tw[(q - 1) * m + k]);
+                for (int q = 1; q < R; q++) a[RX::out_reg(q)] = cmulc(a[RX::out_reg(q)], tw[(q - 1) * m + k]);
             }
-        } else if (MODE == 1) {
-            if (k != 0) {
+            RX::inv(a);
 #pragma unroll
-                for (int q = 1; q < R; q++) a[q] = cmulc(a[q], tw[(q - 1) * m + k]);
-            }
-            SmallDFT<R, true, V>::run(a);
+            for (int s = 0; s < R; s++) buf[base + s * m] = a[s];
         } else {
-            SmallDFT<R, false, V>::run(a);
 #pragma unroll
-            for (int q = 0; q < R; q++) a[q] = cmul(a[q], filt[q * nb + t]);
-            SmallDFT<R, true, V>::run(a);
+            for (int s = 0; s < R; s++) a[s] = buf[base + s * m];
+            RX::fwd(a);
+            if (MODE == 0) {
+                if (k != 0) {
+#pragma unroll
+                    for (int q = 1; q < R; q++) a[RX::out_reg(q)] = cmul(a[RX::out_reg(q)], tw[(q - 1) * m + k]);
+                }
+#pragma unroll
+                for (int q = 0; q < R; q++) buf[base + q * m] = a[RX::out_reg(q)];
+            } else {
+#pragma unroll
+                for (int q = 0; q < R; q++) a[RX::out_reg(q)] = cmul(a[RX::out_reg(q)], filt[q * nb + t]);
+                RX::inv(a);
+#pragma unroll
+                for (int s = 0; s < R; s++) buf[base + s * m] = a[s];
+            }
         }
-#pragma unroll
-        for (int s = 0; s < R; s++) buf[pad16(base + s * m)] = a[s];
     }
 }
 
-template <int MODE, typename V>
+// Radices the row kernel supports; the plan only emits these.  A kernel
+// compiled for blocks of up to 1024 threads (64 registers a thread) holds
+// radices up to 16; the 512-thread variant (128 registers) all of them.
+#define GBSP_RADIX_LIST(X) \
+    X(2) X(3) X(4) X(5) X(7) X(8) X(9) X(12) X(15) X(16) X(20) X(21) X(24) X(25) X(28) X(32) X(35) X(40)
+
+__host__ __device__ constexpr bool radix_supported(int r) {
+    return r == 2 || r == 3 || r == 4 || r == 5 || r == 7 || r == 8 || r == 9 || r == 12 || r == 15 ||
+           r == 16 || r == 20 || r == 21 || r == 24 || r == 25 || r == 28 || r == 32 || r == 35 || r == 40;
+}
+constexpr int MAX_RADIX_NT1024 = 16;
+constexpr int MAX_RADIX_NT512 = 40;
+
+template <int MODE, int MAXR, typename V>
 __device__ __forceinline__ void fft_stage_dispatch(int R, V* buf, int Lp, int m, uint32_t magic,
                                                    const V* tw, const V* filt, int tid, int nthreads) {
     switch (R) {
-        case 2: fft_stage<2, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); break;
-        case 3: fft_stage<3, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); break;
-        case 4: fft_stage<4, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); break;
-        case 5: fft_stage<5, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); break;
-        case 7: fft_stage<7, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); break;
-        case 8: fft_stage<8, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); break;
+#define GBSP_STAGE_CASE(r)                                                               \
+        case r:                                                                          \
+            if constexpr (r <= MAXR) fft_stage<r, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); \
+            break;
+        GBSP_RADIX_LIST(GBSP_STAGE_CASE)
+#undef GBSP_STAGE_CASE
         default: break;
     }
 }

@@ -16,14 +16,19 @@ namespace gbsp {
 
 constexpr int MAX_STAGES = 16;
 constexpr int MAX_CHANNELS = 8;
-constexpr int ROWS_THREADS = 1024;  // k_bluestein_rows block size
 constexpr int P1_THREADS = 512;     // k_twiddle_sum block size
 constexpr int P1_WARPS = P1_THREADS / 32;
-constexpr int P1_KU = 8;            // Bluestein rows per lane in k_twiddle_sum
-constexpr int P1_UBLK = 32 * P1_KU; // Bluestein rows per work item
 constexpr int P1_RESEED = 4;        // exact table lookup every P1_RESEED rows
-constexpr int P1_STAGE_PITCH = P1_WARPS + 1;
-constexpr size_t P1_STAGE_BYTES = (size_t)P1_UBLK * P1_STAGE_PITCH * 8;
+// k_twiddle_sum shapes: KU Bluestein rows per lane (32*KU per work item) and
+// windows of cw consecutive columns cut into at most cw + P1_WARPS tasks
+__host__ __device__ constexpr int p1_vmax(int cw) { return cw + P1_WARPS; }
+__host__ __device__ constexpr int p1_pitch(int cw) { return p1_vmax(cw) + 1; }
+// shared memory before the twiddle table: result tile + per-warp nonzero data
+__host__ __device__ constexpr size_t p1_head_bytes(int ku, int cw) {
+    return (size_t)32 * ku * p1_pitch(cw) * 8 + (size_t)P1_WARPS * 32 * 16;
+}
+constexpr long long WAIT_LIMIT = 1LL << 26;  // bounded spin on an mbarrier (~seconds)
+constexpr int ERR_TIMEOUT = 1;              // bit set in the plan's error word
 
 struct FFTDesc {
     int Lp;                     // channel FFT length
@@ -81,14 +86,16 @@ __device__ __forceinline__ float2 chirp_twiddle(long long c, int q, int cols, in
     return make_float2((float)co, (float)s);
 }
 
-// pre[q][j]  = chirp(c_j) * W_L^{+c_j*q}, c_j = slot_col[j]  (slot order)
-__global__ void k_table_pre(float2* __restrict__ pre, const int* __restrict__ slot_col, int n_slots,
-                            int cols, int L, int K) {
+// pre[q][c] = W_L^{+c*q}  (channel pre-twiddle; the chirp is applied by pass 1)
+__global__ void k_table_pre(float2* __restrict__ pre, int cols, int L, int K) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)K * n_slots) return;
-    int q = (int)(idx / n_slots);
-    int j = (int)(idx - (long)q * n_slots);
-    pre[idx] = chirp_twiddle(slot_col[j], q, cols, L, +1);
+    if (idx >= (long)K * cols) return;
+    int q = (int)(idx / cols);
+    long long c = idx - (long)q * cols;
+    long long cq = (c * (long long)q) % (long long)L;
+    double s, co;
+    sincospi(-2.0 * (double)cq / (double)L, &s, &co);
+    pre[idx] = make_float2((float)co, (float)s);
 }
 
 // post[q][c] = chirp(c) * W_L^{-c*q}  (column order)
@@ -138,43 +145,34 @@ __global__ void k_table_filter_input(double2* __restrict__ bq, int cols, int L, 
     bq[idx] = make_double2(ax, ay);
 }
 
-// One forward DIF stage over K channels in global memory, FP64, twiddles
-// evaluated on the fly.  Used once per plan for the filter spectrum.
-template <int R>
-__device__ __forceinline__ void dif_stage_f64_one(double2* __restrict__ x, int Lp, int m, int t) {
-    int j = t / m, k = t - (t / m) * m;
-    int base = j * R * m + k;
-    long long l = Lp / (R * m);
-    double2 a[R];
-#pragma unroll
-    for (int s = 0; s < R; s++) a[s] = x[base + s * m];
-    SmallDFT<R, false, double2>::run(a);
-#pragma unroll
-    for (int q = 1; q < R; q++) {
-        long long e = ((long long)q * k * l) % Lp;
-        double sn, cs;
-        sincospi(-2.0 * (double)e / (double)Lp, &sn, &cs);
-        a[q] = cmul(a[q], make_double2(cs, sn));
-    }
-#pragma unroll
-    for (int s = 0; s < R; s++) x[base + s * m] = a[s];
-}
-
+// One forward DIF stage (any radix R <= MAX_RADIX) over K channels in global
+// memory, FP64: the R-point DFT by its definition and the stage twiddles,
+// every root evaluated from an exactly reduced integer phase.  Used once per
+// plan for the filter spectrum, so it follows the row kernel's network.
+constexpr int MAX_RADIX = 64;
 __global__ void k_dif_stage_f64(double2* __restrict__ data, int K, int Lp, int R, int m) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int nb = Lp / R;
-    if (idx >= (long)K * nb) return;
+    if (idx >= (long)K * nb || R > MAX_RADIX) return;
     int ch = (int)(idx / nb);
     int t = (int)(idx - (long)ch * nb);
     double2* x = data + (size_t)ch * Lp;
-    switch (R) {
-        case 2: dif_stage_f64_one<2>(x, Lp, m, t); break;
-        case 3: dif_stage_f64_one<3>(x, Lp, m, t); break;
-        case 4: dif_stage_f64_one<4>(x, Lp, m, t); break;
-        case 5: dif_stage_f64_one<5>(x, Lp, m, t); break;
-        case 7: dif_stage_f64_one<7>(x, Lp, m, t); break;
-        case 8: dif_stage_f64_one<8>(x, Lp, m, t); break;
-        default: break;
+    int j = t / m, k = t - (t / m) * m;
+    int base = j * R * m + k;
+    long long l = Lp / (R * m);
+    double2 in[MAX_RADIX];
+    for (int s = 0; s < R; s++) in[s] = x[base + s * m];
+    for (int q = 0; q < R; q++) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int s = 0; s < R; s++) {
+            double sn, cs;
+            sincospi(-2.0 * (double)((s * q) % R) / (double)R, &sn, &cs);
+            acc = cadd(acc, cmul(in[s], make_double2(cs, sn)));
+        }
+        long long e = ((long long)q * k * l) % Lp;
+        double sn, cs;
+        sincospi(-2.0 * (double)e / (double)Lp, &sn, &cs);
+        x[base + q * m] = cmul(acc, make_double2(cs, sn));
     }
 }
 
@@ -192,12 +190,64 @@ __global__ void k_table_filter_final(float2* __restrict__ filt, const double2* _
 }
 
 // ---------------------------------------------------------------------------
-// Pass 1: twiddle sums over each active column's nonzero rows.
+// mbarrier + bulk-copy helpers (inline PTX).  Every wait is bounded: after
+// WAIT_LIMIT polls the kernel records ERR_TIMEOUT in *err and carries on, so
+// no barrier can hang the GPU; the host reports the flag as an error.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// true if the phase completed, false after WAIT_LIMIT polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (long long i = 0; i < WAIT_LIMIT; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// global -> this CTA's shared memory, completion counted on bar
+__device__ __forceinline__ void bulk_copy_g2s(void* dst_smem, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst_smem)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) accesses
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1: twiddle sums over each column's nonzero rows, times the chirp.
 //
-// Columns live in "slots" sorted by degree (descending), so the P1_WARPS
-// columns of one work item have nearly equal nonzero counts.  A work item is
-// (block of P1_UBLK Bluestein rows, group of P1_WARPS slots); warp w owns
-// slot g*P1_WARPS + w and lane l owns rows u = ubase + l + 32*kk (kk < KU).
+// A work item is (block of 32*KU Bluestein rows, window of cw consecutive
+// columns).  On the host each window's nonzeros are cut into at most
+// cw + P1_WARPS tasks: a column of degree d becomes ceil(d / T) contiguous
+// parts with T = max(32, ceil(window nnz / P1_WARPS)), so no task exceeds a
+// warp's fair share.  The warps of the CTA pull tasks from a shared counter
+// longest first; lane l owns rows u = ubase + l + 32*kk.  Each task's sums
+// land in their own column of a shared-memory tile, and the window is written
+// by summing every column's parts in a fixed order (Kahan-compensated when a
+// column has several), so the result is balanced and deterministic.
 //
 // Per nonzero r the lane reduces its phase (u*r) mod rows exactly with an
 // integer multiply-high and reads W_rows^p from the table staged in shared
@@ -205,10 +255,11 @@ __global__ void k_table_filter_final(float2* __restrict__ filt, const double2* _
 // W_rows^{(32*r) mod rows} as a complex multiplier, and every P1_RESEED rows
 // the value is looked up exactly again, so no twiddle is more than
 // P1_RESEED-1 products away from a correctly rounded table entry.  Sums of a
-// batch of 32 nonzeros are added to the column total; for columns with at
-// least kahan_min nonzeros that addition is Kahan-compensated.  Results pass
-// through a shared-memory tile so every S row segment is written as whole
-// 128-byte lines.
+// batch of 32 nonzeros are added to the task total; for tasks of at least
+// kahan_min nonzeros that addition is Kahan-compensated.  The window's
+// results (times chirp[c] when a chirp table is given) leave as whole
+// 512-byte row segments of S, in column order, zero for empty columns --
+// ready for a bulk copy.
 //
 // The reference evaluates __sincosf of a float angle per (u, nonzero), one
 // output row per thread, and writes strided 8-byte values
@@ -223,41 +274,48 @@ __device__ __forceinline__ float2 row_twiddle(const float2* tab, uint32_t p, uin
     return w;
 }
 
-template <typename IDX, bool TAB_HALF, bool BIG>
+// one nonzero as a warp shares it: row, reseed step, and W^{(32*r) mod rows}
+struct NzInfo {
+    uint32_t r, step;
+    float wx, wy;
+};
+
+template <typename IDX, bool TAB_HALF, bool BIG, int KU>
 __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx, int beg, int end,
-                                                 const float2* tab, uint32_t u_lane, uint32_t rows,
-                                                 uint32_t magic, int lane, bool compensated,
-                                                 float2 (&acc)[P1_KU]) {
-    float2 cmp[P1_KU];
+                                                 const float2* tab, NzInfo* info, uint32_t u_lane,
+                                                 uint32_t rows, uint32_t magic, int lane, bool compensated,
+                                                 float2 (&acc)[KU]) {
+    float2 cmp[KU];
 #pragma unroll
-    for (int i = 0; i < P1_KU; i++) { acc[i] = make_float2(0.f, 0.f); cmp[i] = make_float2(0.f, 0.f); }
+    for (int i = 0; i < KU; i++) { acc[i] = make_float2(0.f, 0.f); cmp[i] = make_float2(0.f, 0.f); }
     const uint32_t hr = rows / 2;
     for (int p0 = beg; p0 < end; p0 += 32) {
         const int cnt = min(32, end - p0);
-        uint32_t rl = 0, sl = 0;
-        float2 wl = make_float2(1.f, 0.f);
         if (lane < cnt) {
-            rl = (uint32_t)row_idx[p0 + lane];
-            const uint32_t d = mulmod_rows<BIG>(32u, rl, rows, magic);
-            wl = row_twiddle<TAB_HALF>(tab, d, rows, hr);
-            sl = mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic);
+            const uint32_t r = (uint32_t)row_idx[p0 + lane];
+            const uint32_t d = mulmod_rows<BIG>(32u, r, rows, magic);
+            const float2 wd = row_twiddle<TAB_HALF>(tab, d, rows, hr);
+            const uint32_t st = (KU > P1_RESEED) ? mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic) : 0u;
+            info[lane] = NzInfo{r, st, wd.x, wd.y};
         }
-        float2 blk[P1_KU];
+        __syncwarp();
+        float2 blk[KU];
 #pragma unroll
-        for (int i = 0; i < P1_KU; i++) blk[i] = make_float2(0.f, 0.f);
+        for (int i = 0; i < KU; i++) blk[i] = make_float2(0.f, 0.f);
+#pragma unroll 2
         for (int i = 0; i < cnt; i++) {
-            const uint32_t r = __shfl_sync(0xffffffffu, rl, i);
-            const uint32_t step = __shfl_sync(0xffffffffu, sl, i);
-            const float2 wd = make_float2(__shfl_sync(0xffffffffu, wl.x, i),
-                                          __shfl_sync(0xffffffffu, wl.y, i));
-            uint32_t p = mulmod_rows<BIG>(u_lane, r, rows, magic);
+            const NzInfo z = info[i];  // one broadcast 16-byte load
+            const float2 wd = make_float2(z.wx, z.wy);
+            uint32_t p = mulmod_rows<BIG>(u_lane, z.r, rows, magic);
             float2 w = make_float2(1.f, 0.f);
 #pragma unroll
-            for (int kk = 0; kk < P1_KU; kk++) {
+            for (int kk = 0; kk < KU; kk++) {
                 if (kk % P1_RESEED == 0) {
                     w = row_twiddle<TAB_HALF>(tab, p, rows, hr);
-                    const uint32_t pn = p + step;
-                    p = min(pn, pn - rows);
+                    if (kk + P1_RESEED < KU) {
+                        const uint32_t pn = p + z.step;
+                        p = min(pn, pn - rows);
+                    }
                 } else {
                     w = cmul(w, wd);
                 }
@@ -265,9 +323,10 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
                 blk[kk].y += w.y;
             }
         }
+        __syncwarp();
         if (compensated) {
 #pragma unroll
-            for (int kk = 0; kk < P1_KU; kk++) {
+            for (int kk = 0; kk < KU; kk++) {
                 float y = blk[kk].x - cmp[kk].x;
                 float t = acc[kk].x + y;
                 cmp[kk].x = (t - acc[kk].x) - y;
@@ -279,87 +338,140 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
             }
         } else {
 #pragma unroll
-            for (int kk = 0; kk < P1_KU; kk++) { acc[kk].x += blk[kk].x; acc[kk].y += blk[kk].y; }
+            for (int kk = 0; kk < KU; kk++) { acc[kk].x += blk[kk].x; acc[kk].y += blk[kk].y; }
         }
     }
 }
 
-template <typename IDX, bool TAB_HALF, bool BIG>
-__global__ void __launch_bounds__(P1_THREADS)
-k_twiddle_sum(const int* __restrict__ slot_ptr, const IDX* __restrict__ row_idx, int n_slots,
-              const float2* __restrict__ row_tab, int ntab, int rows, uint32_t magic,
-              int u0, int tile_rows, float2* __restrict__ S, size_t s_pitch, int kahan_min) {
+// win_slot0[w*(cw+1) + lc]: first tile column of window w's column lc
+// (entry cw = tasks in the window); win_task[w*vmax + i] = nonzero range
+// (begin, end) and win_task_col[...] its tile column, longest task first.
+// S row u-u0 gets columns [0, s_cols), zero past cols.
+template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+__global__ void __launch_bounds__(P1_THREADS, 1)
+k_twiddle_sum(const IDX* __restrict__ row_idx, const uint8_t* __restrict__ win_slot0,
+              const int2* __restrict__ win_task, const uint8_t* __restrict__ win_task_col, int cw,
+              int cols, int s_cols, const float2* __restrict__ row_tab, int ntab, int rows, uint32_t magic,
+              const float2* __restrict__ chirp, int u0, int tile_rows, float2* __restrict__ S,
+              size_t s_pitch, int kahan_min) {
+    constexpr int UBLK = 32 * KU;
     extern __shared__ float4 smem_raw[];
+    const int pitch = p1_pitch(cw), vmax = p1_vmax(cw);
     float2* stage = reinterpret_cast<float2*>(smem_raw);
-    float2* tab = stage + P1_UBLK * P1_STAGE_PITCH;
+    NzInfo* info_all = reinterpret_cast<NzInfo*>(stage + (size_t)UBLK * pitch);
+    float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
+    __shared__ int next_task;
+    __shared__ int s_slot0[64 + 1];
+    __shared__ float2 s_chirp[64];
     for (int i = threadIdx.x; i < ntab; i += blockDim.x) tab[i] = row_tab[i];
+    if (threadIdx.x == 0) next_task = 0;
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int n_ublk = (tile_rows + P1_UBLK - 1) / P1_UBLK;
-    const int n_grp = (n_slots + P1_WARPS - 1) / P1_WARPS;
-    const long nitems = (long)n_ublk * n_grp;
+    NzInfo* info = info_all + (threadIdx.x >> 5) * 32;
+    const int n_ublk = (tile_rows + UBLK - 1) / UBLK;
+    const int n_win = (s_cols + cw - 1) / cw;
+    const long nitems = (long)n_ublk * n_win;
 
     for (long it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int ub = (int)(it / n_grp);
-        const int g = (int)(it - (long)ub * n_grp);
-        const int ul0 = ub * P1_UBLK;
-        const int j = g * P1_WARPS + warp;
-        if (j < n_slots) {
-            const uint32_t u_lane = (uint32_t)(u0 + ul0 + lane) % (uint32_t)rows;
-            const int beg = slot_ptr[j], end = slot_ptr[j + 1];
-            float2 acc[P1_KU];
-            column_sums_warp<IDX, TAB_HALF, BIG>(row_idx, beg, end, tab, u_lane, (uint32_t)rows, magic,
-                                                 lane, kahan_min > 0 && end - beg >= kahan_min, acc);
+        const int ub = (int)(it / n_win);
+        const int w = (int)(it - (long)ub * n_win);
+        const int ul0 = ub * UBLK;
+        const int c0 = w * cw;
+        const uint8_t* slot0 = win_slot0 + (size_t)w * (cw + 1);
+        if (threadIdx.x <= cw) s_slot0[threadIdx.x] = slot0[threadIdx.x];
+        if (threadIdx.x < cw) {
+            const int c = c0 + threadIdx.x;
+            s_chirp[threadIdx.x] = (chirp && c < cols) ? chirp[c] : make_float2(1.f, 0.f);
+        }
+        const int ntask = slot0[cw];
+        const uint32_t u_lane = (uint32_t)(u0 + ul0 + lane) % (uint32_t)rows;
+        for (;;) {
+            int i = 0;
+            if (lane == 0) i = atomicAdd(&next_task, 1);
+            i = __shfl_sync(0xffffffffu, i, 0);
+            if (i >= ntask) break;
+            const int2 range = win_task[(size_t)w * vmax + i];
+            const int col = win_task_col[(size_t)w * vmax + i];
+            float2 acc[KU];
+            column_sums_warp<IDX, TAB_HALF, BIG, KU>(row_idx, range.x, range.y, tab, info, u_lane,
+                                                     (uint32_t)rows, magic, lane,
+                                                     kahan_min > 0 && range.y - range.x >= kahan_min, acc);
 #pragma unroll
-            for (int kk = 0; kk < P1_KU; kk++) stage[(lane + 32 * kk) * P1_STAGE_PITCH + warp] = acc[kk];
+            for (int kk = 0; kk < KU; kk++) stage[(lane + 32 * kk) * pitch + col] = acc[kk];
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < P1_UBLK * P1_WARPS; e += blockDim.x) {
-            const int row = e / P1_WARPS, col = e - (e / P1_WARPS) * P1_WARPS;
-            const int ul = ul0 + row, jj = g * P1_WARPS + col;
-            if (ul < tile_rows && jj < n_slots)
-                S[(size_t)ul * s_pitch + jj] = stage[row * P1_STAGE_PITCH + col];
+        const int ncol = min(cw, s_cols - c0);
+        for (int e = threadIdx.x; e < UBLK * cw; e += blockDim.x) {
+            const int row = e / cw, lc = e - (e / cw) * cw;
+            const int ul = ul0 + row;
+            if (ul >= tile_rows || lc >= ncol) continue;
+            const int a = s_slot0[lc], b = s_slot0[lc + 1];
+            const float2* srow = stage + row * pitch;
+            float2 v = make_float2(0.f, 0.f);
+            if (b - a == 1) {
+                v = srow[a];
+            } else {
+                float2 comp = make_float2(0.f, 0.f);
+                for (int k = a; k < b; k++) {  // parts in a fixed order, compensated
+                    float y = srow[k].x - comp.x;
+                    float t = v.x + y;
+                    comp.x = (t - v.x) - y;
+                    v.x = t;
+                    y = srow[k].y - comp.y;
+                    t = v.y + y;
+                    comp.y = (t - v.y) - y;
+                    v.y = t;
+                }
+            }
+            S[(size_t)ul * s_pitch + c0 + lc] = cmul(v, s_chirp[lc]);
         }
+        if (threadIdx.x == 0) next_task = 0;
         __syncthreads();
     }
 }
 
 // ---------------------------------------------------------------------------
 // Bluestein rows.  Channel q of K (the CTA's rank in its cluster) holds
-//   y_q[n] = sum_{c = n mod Lp} pre[q][c] * S[u][c]          (n < Lp)
-// runs the forward DIF FFT of length Lp, multiplies by the channel's filter
-// spectrum (digit-reversed, scaled by 1/L), and runs the inverse DIT FFT,
-// leaving Z_q[n] in natural order.  The length-L convolution result is then
+//   y_q[n] = sum_{c = n mod Lp} pre[q][c] * x[u][c]          (n < Lp)
+// where x = S (pass 1 already multiplied by the chirp), runs the forward DIF
+// FFT of length Lp, multiplies by the channel's filter spectrum (in the
+// network's digit-reversed order, scaled by 1/L), and runs the inverse DIT
+// FFT, leaving Z_q[n] in natural order.  The length-L convolution result is
 //   y[c] = sum_q post[q][c] * Z_q[c mod Lp]
 // read across the cluster's shared memories (DSMEM).  Since the 2-D input is
 // real, F[rows-u][v] = conj(F[u][(cols-v) mod cols]), so one Bluestein row u
 // (u <= rows/2) writes output rows u and rows-u, each with 16-byte stores of
 // two complex values.
 //
-// Shared memory: the padded row buffer, then the twiddles of stages >= 1
-// (loaded once per CTA); stage 0's twiddles stream from L2.
+// The input row arrives with one bulk copy (cp.async.bulk) straight into the
+// FFT buffer whenever it fits (columns rounded up to even <= Lp); otherwise
+// (several columns folding onto one slot) it is added section by section.
+//
+// Shared memory: the row buffer, then the twiddles of stages >= 1 (loaded
+// once per CTA); stage 0's twiddles stream from L2.
 //
 // The reference runs 2F+4 launches per tile of rows with a global round trip
 // per stage (src/sparse_fft_bluestein.cu:2327-2370) and writes 8-byte stores
 // in bluestein_finalize_kernel (:469-486).
 // ---------------------------------------------------------------------------
-template <bool CLUSTER>
-__global__ void __launch_bounds__(ROWS_THREADS, 1)
-k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_slots,
-                 const int* __restrict__ slot_col, const float2* __restrict__ pre,
+template <int NTMAX>
+__global__ void __launch_bounds__(NTMAX, 1)
+k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, const float2* __restrict__ pre,
                  const float2* __restrict__ post, const float2* __restrict__ filt,
                  const float2* __restrict__ fft_tw, FFTDesc fd, int K, int rows, int cols,
-                 int u0, int tile_rows, float2* __restrict__ out, size_t out_pitch) {
+                 int u0, int tile_rows, float2* __restrict__ out, size_t out_pitch, int* err) {
     extern __shared__ float4 smem_raw[];
+    __shared__ uint64_t in_bar;
     float2* buf = reinterpret_cast<float2*>(smem_raw);
     const int Lp = fd.Lp;
-    const int Lpad = padded_len(Lp);
-    float2* twr = buf + Lpad;
+    float2* twr = buf + Lp;
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int i = tid; i < fd.rest_len; i += nt) twr[i] = fft_tw[fd.rest_base + i];
+    if (tid == 0) mbar_init(&in_bar, 1);
 
+    constexpr int MAXR = (NTMAX > 512) ? MAX_RADIX_NT1024 : MAX_RADIX_NT512;
+    const bool CLUSTER = K > 1;  // K > 1 only in launches with a K-CTA cluster dimension
     int q = 0, cid = blockIdx.x, ncl = gridDim.x;
     const float2* zsrc[MAX_CHANNELS];
     if (CLUSTER) {
@@ -373,53 +485,58 @@ k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_slots,
     } else {
         zsrc[0] = buf;
     }
-    const float2* preq = pre + (size_t)q * n_slots;
+    const float2* preq = pre + (size_t)q * cols;
     const float2* filtq = filt + (size_t)q * Lp;
     const int half_slots = (int)(out_pitch >> 1);
     const int hc = cols / 2;
-    const bool wrap_in = cols > Lp;
+    const int cols_even = (cols + 1) & ~1;
+    const bool bulk_in = cols_even <= Lp;
     // stage 0 twiddles stream from global memory, the rest sit in shared memory
     auto tw_of = [&](int s) -> const float2* {
         return (s == 0) ? fft_tw + fd.twoff[0] : twr + (fd.twoff[s] - fd.rest_base);
     };
+    uint32_t parity = 0;
+    bool timed_out = false;
+    __syncthreads();
 
     for (int t = cid; t < tile_rows; t += ncl) {
         const int u = u0 + t;
-        for (int i = tid; i < Lpad; i += nt) buf[i] = make_float2(0.f, 0.f);
-        __syncthreads();
         const float2* srow = S + (size_t)t * s_pitch;
-        if (!wrap_in) {
-            for (int j = tid; j < n_slots; j += nt) {
-                const int c = slot_col[j];
-                buf[pad16(c)] = cmul(srow[j], preq[j]);
+        if (bulk_in) {
+            if (tid == 0) {
+                fence_proxy_async_smem();
+                mbar_expect_tx(&in_bar, (uint32_t)cols_even * 8u);
+                bulk_copy_g2s(buf, srow, (uint32_t)cols_even * 8u, &in_bar);
             }
+            for (int i = cols_even + tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
+            if (!mbar_wait_bounded(&in_bar, parity)) timed_out = true;
+            parity ^= 1u;
+            if (q != 0)  // channel pre-twiddle (channel 0's is 1)
+                for (int c = tid; c < cols; c += nt) buf[c] = cmul(buf[c], __ldg(preq + c));
             __syncthreads();
         } else {
+            for (int i = tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
+            __syncthreads();
             // several input columns fold onto one slot: add section by section
-            for (int sec = 0; sec * Lp < cols; sec++) {
-                const int lo = sec * Lp, hi = lo + Lp;
-                for (int j = tid; j < n_slots; j += nt) {
-                    const int c = slot_col[j];
-                    if (c >= lo && c < hi) {
-                        float2* d = buf + pad16(c - lo);
-                        *d = cadd(*d, cmul(srow[j], preq[j]));
-                    }
-                }
+            for (int lo = 0; lo < cols; lo += Lp) {
+                const int hi = min(cols, lo + Lp);
+                for (int c = lo + tid; c < hi; c += nt)
+                    buf[c - lo] = cadd(buf[c - lo], cmul(__ldcs(srow + c), __ldg(preq + c)));
                 __syncthreads();
             }
         }
         // forward DIF, filter multiply fused with the last stage, inverse DIT
         const int S1 = fd.nst - 1;
         for (int s = 0; s < S1; s++) {
-            fft_stage_dispatch<0>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                  (const float2*)nullptr, tid, nt);
+            fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
+                                        (const float2*)nullptr, tid, nt);
             __syncthreads();
         }
-        fft_stage_dispatch<2>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
+        fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
         __syncthreads();
         for (int s = S1 - 1; s >= 0; s--) {
-            fft_stage_dispatch<1>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                  (const float2*)nullptr, tid, nt);
+            fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
+                                        (const float2*)nullptr, tid, nt);
             __syncthreads();
         }
         if (CLUSTER) cg::this_cluster().sync();
@@ -439,14 +556,13 @@ k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_slots,
                 float2 val = make_float2(0.f, 0.f);
                 if (vv <= hc) {
                     const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
-                    int n = c;
-                    while (n >= Lp) n -= Lp;
-                    const int pn = pad16(n);
                     if (CLUSTER) {
+                        int n = c;
+                        while (n >= Lp) n -= Lp;
                         for (int qq = 0; qq < K; qq++)
-                            val = cadd(val, cmul(zsrc[qq][pn], post[(size_t)qq * cols + c]));
+                            val = cadd(val, cmul(zsrc[qq][n], __ldg(post + (size_t)qq * cols + c)));
                     } else {
-                        val = cmul(buf[pn], post[c]);
+                        val = cmul(buf[c], __ldg(post + c));
                     }
                     if (sel) val.y = -val.y;
                 }
@@ -454,10 +570,16 @@ k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, int n_slots,
             }
             const int row = sel ? u2 : u;
             float4* dst = reinterpret_cast<float4*>(out + (size_t)row * out_pitch + v);
-            *dst = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+            __stcs(dst, make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
         }
         if (CLUSTER) cg::this_cluster().sync();
         else __syncthreads();
+    }
+    if (timed_out) {
+        atomicOr(err, ERR_TIMEOUT);
+        // a copy that never signalled may still be in flight: wait once more
+        // (bounded) before the shared memory is released
+        mbar_wait_bounded(&in_bar, parity ^ 1u);
     }
 }
 

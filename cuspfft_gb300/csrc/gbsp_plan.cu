@@ -1,11 +1,12 @@
 // gbsp_plan.cu -- plans and execution behind the C ABI (include/gbspfft.h).
 //
-// A plan owns everything the timed loop reads: the uploaded CSC (columns
-// re-ordered into degree-sorted slots), the FP64-built tables rounded to
-// FP32, and the pass-1 scratch tile.  Execution is two launches per tile of
+// A plan owns everything the timed loop reads: the uploaded CSC, the
+// per-window column order of pass 1, the FP64-built tables rounded to FP32,
+// and the pass-1 scratch tile.  Execution is two launches per tile of
 // Bluestein rows: k_twiddle_sum (pass 1) and k_bluestein_rows (convolution +
 // R2C writer).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -27,13 +28,16 @@ struct gbsp_plan_s {
     gbsp::FFTDesc fd{};
     int half_rows = 0, u_tile = 0, out_cols = 0, out_pitch = 0;
     int idx_bytes = 2, tab_half = 0, big = 0, kahan_min = 64, ntab = 0;
+    int p1_ku = 8, p1_cw = 32;       // pass-1 rows per lane (x32 per item) and window width
     uint32_t rows_magic = 0;
-    std::vector<int> slot_col_host;  // column of each slot
-    int* d_slot_ptr = nullptr;       // n_active + 1
-    void* d_row_idx = nullptr;       // nnz, u16 or u32, grouped by slot
-    int* d_slot_col = nullptr;       // n_active
+    void* d_row_idx = nullptr;       // nnz, u16 or u32, column order
+    uint8_t* d_win_slot0 = nullptr;  // pass-1 windows: first tile column of each column
+    int2* d_win_task = nullptr;      // pass-1 windows: nonzero range of each task
+    uint8_t* d_win_task_col = nullptr;  // pass-1 windows: tile column of each task
+    int s_cols = 0;                  // columns pass 1 writes per S row (cols rounded up to even)
+    int* d_err = nullptr;            // kernel error flags (bounded waits that timed out)
     float2* d_rowtab = nullptr;
-    float2* d_pre = nullptr;         // K x n_active (slot order)
+    float2* d_pre = nullptr;         // K x cols channel pre-twiddles W_L^{c*q}
     float2* d_post = nullptr;        // K x cols
     float2* d_filt = nullptr;        // K x Lp (fused-stage thread order)
     float2* d_fftw = nullptr;        // stage twiddles, q-major blocks
@@ -41,7 +45,7 @@ struct gbsp_plan_s {
     size_t s_pitch = 0;
     int p1_grid = 0;
     size_t p1_smem = 0;
-    int rows_grid = 0;
+    int rows_grid = 0, rows_threads = 1024, rows_ntmax = 1024;
     size_t rows_smem = 0;
     size_t device_bytes = 0;
     std::vector<void*> allocs;
@@ -78,24 +82,15 @@ void free_plan(gbsp_plan_s* p) {
 
 inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-// Radix plan for a 7-smooth channel length: radix-8 stages while three or
-// more factors of 2 remain, then 4 or 2, then 3s, 5s and 7s (an odd radix
-// last keeps the span-1 stage free of shared-memory bank conflicts).
-int build_fft_desc(int Lp, gbsp::FFTDesc* fd) {
-    int e2 = 0, e3 = 0, e5 = 0, e7 = 0, x = Lp;
-    while (x % 2 == 0) { x /= 2; e2++; }
-    while (x % 3 == 0) { x /= 3; e3++; }
-    while (x % 5 == 0) { x /= 5; e5++; }
-    while (x % 7 == 0) { x /= 7; e7++; }
-    if (x != 1) return GBSP_ERR_UNSUPPORTED;
-    std::vector<int> rs;
-    while (e2 >= 3) { rs.push_back(8); e2 -= 3; }
-    if (e2 == 2) rs.push_back(4);
-    if (e2 == 1) rs.push_back(2);
-    for (int i = 0; i < e3; i++) rs.push_back(3);
-    for (int i = 0; i < e5; i++) rs.push_back(5);
-    for (int i = 0; i < e7; i++) rs.push_back(7);
+// Stage descriptor for a given radix sequence (product must be Lp).
+int build_fft_desc(int Lp, const std::vector<int>& rs, gbsp::FFTDesc* fd) {
     if ((int)rs.size() > gbsp::MAX_STAGES || rs.empty()) return GBSP_ERR_UNSUPPORTED;
+    long prod = 1;
+    for (int r : rs) {
+        if (!gbsp::radix_supported(r)) return GBSP_ERR_UNSUPPORTED;
+        prod *= r;
+    }
+    if (prod != Lp) return GBSP_ERR_UNSUPPORTED;
     fd->Lp = Lp;
     fd->nst = (int)rs.size();
     int l = 1, off = 0;
@@ -104,7 +99,10 @@ int build_fft_desc(int Lp, gbsp::FFTDesc* fd) {
         const int m = Lp / (l * R);
         fd->R[s] = R;
         fd->m[s] = m;
-        fd->magic[s] = (m <= 1) ? 0u : (uint32_t)(((1ull << 32) + (uint64_t)m - 1) / (uint64_t)m);
+        // divisor of the stage's thread -> butterfly mapping (see fft_stage)
+        const int lcount = Lp / (R * m);
+        const int div = (m == 1) ? 0 : (gbsp::stage_j_fastest(R, m, lcount) ? lcount : m);
+        fd->magic[s] = (div <= 1) ? 0u : (uint32_t)(((1ull << 32) + (uint64_t)div - 1) / (uint64_t)div);
         fd->twoff[s] = off;
         off += (R - 1) * m;
         l *= R;
@@ -117,12 +115,104 @@ int build_fft_desc(int Lp, gbsp::FFTDesc* fd) {
 int fft_tw_count(const gbsp::FFTDesc& fd) { return fd.rest_base + fd.rest_len; }
 
 size_t rows_smem_bytes(const gbsp::FFTDesc& fd) {
-    return ((size_t)gbsp::padded_len(fd.Lp) + (size_t)fd.rest_len) * sizeof(float2);
+    return ((size_t)fd.Lp + (size_t)fd.rest_len) * sizeof(float2);
 }
 
-template <typename IDX, bool HALF, bool BIG>
+// ---- radix planning -------------------------------------------------------
+// Every multiset of supported radices whose product is the channel length
+// (at most 7 stages) is ordered even radices first, odd radices last (an odd
+// radix at span 1 keeps the last stage free of bank conflicts) and scored by
+// a model of one row's work on a block of nt threads: thread slots actually
+// occupied (ceil(butterflies / nt) rounds of nt threads x radix), a cost per
+// barrier, a penalty for strided shared-memory patterns, and a small one for
+// few resident warps.  The exhaustive tuner can override the choice.
+const int kRadices[] = {49, 40, 35, 32, 28, 25, 24, 21, 20, 16, 15, 14, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+
+void factorizations(int rem, int maxr, std::vector<int>& cur, std::vector<std::vector<int>>& out) {
+    if (rem == 1) {
+        if (!cur.empty()) out.push_back(cur);
+        return;
+    }
+    if ((int)cur.size() >= 7) return;
+    for (int r : kRadices) {
+        if (r > maxr || rem % r) continue;
+        cur.push_back(r);
+        factorizations(rem / r, r, cur, out);
+        cur.pop_back();
+    }
+}
+
+std::vector<int> order_radices(std::vector<int> rs) {
+    std::stable_sort(rs.begin(), rs.end(), [](int a, int b) {
+        const bool ea = (a % 2 == 0), eb = (b % 2 == 0);
+        if (ea != eb) return ea;
+        return a > b;
+    });
+    return rs;
+}
+
+// largest radix a block of the given maximum size can hold in registers
+inline int max_radix_for(int nt_max) { return nt_max > 512 ? gbsp::MAX_RADIX_NT1024 : gbsp::MAX_RADIX_NT512; }
+
+double rows_cost(const gbsp::FFTDesc& fd, int nt) {
+    double cost = 0.0;
+    for (int s = 0; s < fd.nst; s++) {
+        const int R = fd.R[s], m = fd.m[s], nb = fd.Lp / R, l = nb / m;
+        const double rounds = std::ceil((double)nb / (double)nt);
+        double per = rounds * nt * R * (1.0 + 0.08 * std::log2((double)R));
+        const bool strided = (m == 1 && R % 2 == 0) ||
+                             (m > 1 && m < 16 && l > 1 && !gbsp::stage_j_fastest(R, m, l));
+        if (strided) per *= 1.5;
+        per += 0.25 * fd.Lp;
+        cost += (s == fd.nst - 1) ? 1.6 * per : 2.0 * per;
+    }
+    return cost * (1.0 + 0.15 * 512.0 / nt);
+}
+
+struct RadixPlan {
+    gbsp::FFTDesc fd{};
+    int nt = 0;
+    double cost = 1e300;
+};
+
+// Best radix sequence and block size for channel length Lp within the
+// shared-memory budget; returns false if nothing fits.
+bool plan_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt, RadixPlan* best) {
+    std::vector<std::vector<int>> cands;
+    if (radix_opt && radix_opt[0] > 0) {
+        std::vector<int> rs;
+        for (int i = 0; i < 8 && radix_opt[i] > 0; i++) rs.push_back(radix_opt[i]);
+        cands.push_back(rs);
+    } else {
+        std::vector<int> cur;
+        factorizations(Lp, 64, cur, cands);
+        for (auto& c : cands) c = order_radices(c);
+    }
+    bool found = false;
+    for (const auto& rs : cands) {
+        gbsp::FFTDesc fd{};
+        if (build_fft_desc(Lp, rs, &fd) != GBSP_OK) continue;
+        if (rows_smem_bytes(fd) > smem_cap) continue;
+        const int rmax = *std::max_element(rs.begin(), rs.end());
+        const int nt_hi = rmax > max_radix_for(1024) ? 512 : 1024;
+        if (rmax > max_radix_for(512)) continue;
+        for (int nt = 64; nt <= nt_hi; nt += 32) {
+            if (nt_opt > 0 && nt != nt_opt) continue;
+            const double c = rows_cost(fd, nt);
+            if (c < best->cost) {
+                best->cost = c;
+                best->fd = fd;
+                best->nt = nt;
+                found = true;
+            }
+        }
+    }
+    return found;
+}
+
+template <typename IDX, bool HALF, bool BIG, int KU>
 int p1_prepare(gbsp_plan_s* p, int sms) {
-    auto kern = gbsp::k_twiddle_sum<IDX, HALF, BIG>;
+    auto kern = gbsp::k_twiddle_sum<IDX, HALF, BIG, KU>;
     GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->p1_smem));
     int nb = 0;
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, gbsp::P1_THREADS, p->p1_smem));
@@ -131,69 +221,131 @@ int p1_prepare(gbsp_plan_s* p, int sms) {
     return GBSP_OK;
 }
 
-template <typename IDX, bool HALF, bool BIG>
-void p1_launch(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pitch, cudaStream_t st) {
-    gbsp::k_twiddle_sum<IDX, HALF, BIG><<<p->p1_grid, gbsp::P1_THREADS, p->p1_smem, st>>>(
-        p->d_slot_ptr, (const IDX*)p->d_row_idx, p->n_active, p->d_rowtab, p->ntab, p->rows,
-        p->rows_magic, u0, n, S, s_pitch, p->kahan_min);
+template <typename IDX, bool HALF, bool BIG, int KU>
+void p1_launch(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pitch, const float2* chirp,
+               cudaStream_t st) {
+    gbsp::k_twiddle_sum<IDX, HALF, BIG, KU><<<p->p1_grid, gbsp::P1_THREADS, p->p1_smem, st>>>(
+        (const IDX*)p->d_row_idx, p->d_win_slot0, p->d_win_task, p->d_win_task_col, p->p1_cw, p->cols,
+        p->s_cols, p->d_rowtab, p->ntab, p->rows, p->rows_magic, chirp, u0, n, S, s_pitch, p->kahan_min);
 }
 
 // prepare == true: set attributes and grid; false: launch
-template <bool HALF, bool BIG>
-int p1_dispatch_idx(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
-                    cudaStream_t st) {
-    if (p->idx_bytes == 2) {
-        if (prepare) return p1_prepare<uint16_t, HALF, BIG>(p, sms);
-        p1_launch<uint16_t, HALF, BIG>(p, u0, n, S, sp, st);
+template <typename IDX, bool HALF, bool BIG>
+int p1_dispatch_ku(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
+                   const float2* chirp, cudaStream_t st) {
+    if (p->p1_ku == 8) {
+        if (prepare) return p1_prepare<IDX, HALF, BIG, 8>(p, sms);
+        p1_launch<IDX, HALF, BIG, 8>(p, u0, n, S, sp, chirp, st);
     } else {
-        if (prepare) return p1_prepare<uint32_t, HALF, BIG>(p, sms);
-        p1_launch<uint32_t, HALF, BIG>(p, u0, n, S, sp, st);
+        if (prepare) return p1_prepare<IDX, HALF, BIG, 4>(p, sms);
+        p1_launch<IDX, HALF, BIG, 4>(p, u0, n, S, sp, chirp, st);
     }
     return GBSP_OK;
 }
 
-int p1_dispatch(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
-                cudaStream_t st) {
-    if (p->tab_half) {
-        if (p->big) return p1_dispatch_idx<true, true>(p, prepare, sms, u0, n, S, sp, st);
-        return p1_dispatch_idx<true, false>(p, prepare, sms, u0, n, S, sp, st);
-    }
-    if (p->big) return p1_dispatch_idx<false, true>(p, prepare, sms, u0, n, S, sp, st);
-    return p1_dispatch_idx<false, false>(p, prepare, sms, u0, n, S, sp, st);
+// 16-bit indices only occur with rows <= 65536 (no 64-bit phase products)
+template <bool HALF>
+int p1_dispatch_half(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
+                     const float2* chirp, cudaStream_t st) {
+    if (p->idx_bytes == 2) return p1_dispatch_ku<uint16_t, HALF, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
+    if (p->big) return p1_dispatch_ku<uint32_t, HALF, true>(p, prepare, sms, u0, n, S, sp, chirp, st);
+    return p1_dispatch_ku<uint32_t, HALF, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
 }
 
-int launch_pass1(const gbsp_plan_s* p, int u0, int n, float2* S, size_t sp, cudaStream_t st) {
-    p1_dispatch(const_cast<gbsp_plan_s*>(p), false, 0, u0, n, S, sp, st);
+int p1_dispatch(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
+                const float2* chirp, cudaStream_t st) {
+    return p->tab_half ? p1_dispatch_half<true>(p, prepare, sms, u0, n, S, sp, chirp, st)
+                       : p1_dispatch_half<false>(p, prepare, sms, u0, n, S, sp, chirp, st);
+}
+
+// chirp == nullptr gives the raw column sums (gbsp_column_sums)
+int launch_pass1(const gbsp_plan_s* p, int u0, int n, float2* S, size_t sp, const float2* chirp,
+                 cudaStream_t st) {
+    p1_dispatch(const_cast<gbsp_plan_s*>(p), false, 0, u0, n, S, sp, chirp, st);
     GB_CUDA(cudaGetLastError());
+    return GBSP_OK;
+}
+
+// Launch configuration of the row kernel: a plain grid for one channel, a
+// cluster of K CTAs per row otherwise.  NTMAX is the compiled block-size
+// bound (1024: 64 registers a thread; 512: 128, for radices above 16); the
+// block itself has p->rows_threads threads.
+template <bool CL>
+cudaLaunchConfig_t rows_config(const gbsp_plan_s* p, unsigned grid, unsigned nt, cudaStream_t st,
+                               cudaLaunchAttribute* attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(nt);
+    cfg.dynamicSmemBytes = p->rows_smem;
+    cfg.stream = st;
+    if (CL) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = p->K;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    return cfg;
+}
+
+// Sets the kernel's shared-memory limit and returns how many CTAs (K == 1) or
+// clusters (K > 1) of p->rows_threads threads can be resident at once.
+template <bool CL, int NTMAX>
+int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
+    auto kern = gbsp::k_bluestein_rows<NTMAX>;
+    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->rows_smem));
+    *cap = 0;
+    if (!CL) {
+        int nb = 0;
+        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, p->rows_threads, p->rows_smem));
+        *cap = nb * sms;
+    } else {
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)(p->K * sms), p->rows_threads, nullptr, attr);
+        GB_CUDA(cudaOccupancyMaxActiveClusters(cap, kern, &cfg));
+    }
+    return GBSP_OK;
+}
+
+template <bool CL, int NTMAX>
+int rows_launch_t(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch, cudaStream_t st) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>, (const float2*)p->d_S,
+                               p->s_pitch, (const float2*)p->d_pre, (const float2*)p->d_post,
+                               (const float2*)p->d_filt, (const float2*)p->d_fftw, p->fd, p->K,
+                               p->rows, p->cols, u0, n, (float2*)d_out, out_pitch, p->d_err));
     return GBSP_OK;
 }
 
 int launch_rows(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch,
                 cudaStream_t st) {
-    if (p->K == 1) {
-        gbsp::k_bluestein_rows<false><<<p->rows_grid, gbsp::ROWS_THREADS, p->rows_smem, st>>>(
-            p->d_S, p->s_pitch, p->n_active, p->d_slot_col, p->d_pre, p->d_post, p->d_filt,
-            p->d_fftw, p->fd, 1, p->rows, p->cols, u0, n, (float2*)d_out, out_pitch);
-        GB_CUDA(cudaGetLastError());
-        return GBSP_OK;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    cfg.gridDim = dim3(p->rows_grid);
-    cfg.blockDim = dim3(gbsp::ROWS_THREADS);
-    cfg.dynamicSmemBytes = p->rows_smem;
-    cfg.stream = st;
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = p->K;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<true>, (const float2*)p->d_S,
-                               p->s_pitch, p->n_active, (const int*)p->d_slot_col,
-                               (const float2*)p->d_pre, (const float2*)p->d_post,
-                               (const float2*)p->d_filt, (const float2*)p->d_fftw, p->fd, p->K,
-                               p->rows, p->cols, u0, n, (float2*)d_out, out_pitch));
+    if (p->K == 1)
+        return p->rows_ntmax == 512 ? rows_launch_t<false, 512>(p, u0, n, d_out, out_pitch, st)
+                                    : rows_launch_t<false, 1024>(p, u0, n, d_out, out_pitch, st);
+    return p->rows_ntmax == 512 ? rows_launch_t<true, 512>(p, u0, n, d_out, out_pitch, st)
+                                : rows_launch_t<true, 1024>(p, u0, n, d_out, out_pitch, st);
+}
+
+// Block size and radices are already chosen; pick the compiled variant and
+// size the persistent grid.
+int rows_prepare(gbsp_plan_s* p, int sms) {
+    int rmax = 0;
+    for (int s = 0; s < p->fd.nst; s++) rmax = std::max(rmax, p->fd.R[s]);
+    p->rows_ntmax = (rmax > max_radix_for(1024) || p->rows_threads <= 512) ? 512 : 1024;
+    if (p->rows_threads > p->rows_ntmax || p->rows_threads < 32 || p->rows_threads % 32)
+        return set_error(GBSP_ERR_INVALID, "rows_threads must be a multiple of 32, at most 512 when a "
+                                           "radix exceeds 16, at most 1024 otherwise");
+    int cap = 0, rc;
+    const bool cl = p->K > 1;
+    if (p->rows_ntmax == 512)
+        rc = cl ? rows_capacity<true, 512>(p, sms, &cap) : rows_capacity<false, 512>(p, sms, &cap);
+    else
+        rc = cl ? rows_capacity<true, 1024>(p, sms, &cap) : rows_capacity<false, 1024>(p, sms, &cap);
+    if (rc) return rc;
+    if (cap < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row kernel does not fit on an SM");
+    p->rows_grid = cap * p->K;
     return GBSP_OK;
 }
 
@@ -233,15 +385,18 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     if (L < 2) L = 2;
     if (L > (1L << 28)) return set_error(GBSP_ERR_UNSUPPORTED, "fft_len too large");
     p->L = (int)L;
-    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 20736;
+    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 24000;
+    const int nt_opt = o ? o->rows_threads : 0;
+    if (nt_opt < 0 || nt_opt % 32 || nt_opt > 1024)
+        return set_error(GBSP_ERR_INVALID, "rows_threads must be 0 or a multiple of 32 up to 1024");
     p->K = 0;
     for (int k = 1; k <= gbsp::MAX_CHANNELS && !p->K; k++) {
         if (L % k || L / k > maxLp || L / k < 2) continue;
-        gbsp::FFTDesc fd{};
-        if (build_fft_desc((int)(L / k), &fd) != GBSP_OK) continue;
-        if (rows_smem_bytes(fd) > smem_cap) continue;
+        RadixPlan rp;
+        if (!plan_radices((int)(L / k), smem_cap, o ? o->radix : nullptr, nt_opt, &rp)) continue;
         p->K = k;
-        p->fd = fd;
+        p->fd = rp.fd;
+        p->rows_threads = rp.nt;
     }
     if (p->K == 0)
         return set_error(GBSP_ERR_UNSUPPORTED,
@@ -262,85 +417,94 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->big = p->rows > 65535;
     p->rows_magic = (p->rows >= 2) ? (uint32_t)(((1ull << 32) + (uint64_t)p->rows - 1) / (uint64_t)p->rows) : 0u;
 
-    // ---- pass-1 configuration: staging tile + twiddle table in shared memory
-    const size_t tab_budget = smem_cap - gbsp::P1_STAGE_BYTES - 256;
-    if ((size_t)p->rows * sizeof(float2) <= std::min<size_t>(tab_budget, 160 * 1024)) {
-        p->tab_half = 0;
-        p->ntab = p->rows;
-    } else if ((size_t)(p->rows / 2 + 1) * sizeof(float2) <= tab_budget) {
-        p->tab_half = 1;
-        p->ntab = p->rows / 2 + 1;
-    } else {
-        return set_error(GBSP_ERR_UNSUPPORTED, "rows too large for a shared-memory twiddle table");
+    // ---- pass-1 configuration: result tile + twiddle table in shared memory.
+    // Preference order: 256-row items with 32-column windows, full table, then
+    // half table; then 128-row items with 64- or 32-column windows.
+    const int tmode = o ? o->row_table_mode : 0;
+    if (tmode < 0 || tmode > 2) return set_error(GBSP_ERR_INVALID, "row_table_mode must be 0, 1 or 2");
+    {
+        struct Shape { int ku, cw, half; };
+        const Shape shapes[] = {{8, 32, 0}, {8, 32, 1}, {4, 64, 0}, {4, 32, 0}, {4, 64, 1}, {4, 32, 1}};
+        bool ok = false;
+        for (const Shape& sh : shapes) {
+            if ((tmode == 1 && sh.half) || (tmode == 2 && !sh.half)) continue;
+            const size_t ntab = sh.half ? (size_t)(p->rows / 2 + 1) : (size_t)p->rows;
+            const size_t bytes = gbsp::p1_head_bytes(sh.ku, sh.cw) + ntab * sizeof(float2);
+            if (bytes + 1024 > smem_cap) continue;  // static shared variables
+            p->p1_ku = sh.ku;
+            p->p1_cw = sh.cw;
+            p->tab_half = sh.half;
+            p->ntab = (int)ntab;
+            p->p1_smem = bytes;
+            ok = true;
+            break;
+        }
+        if (!ok) return set_error(GBSP_ERR_UNSUPPORTED, "rows too large for a shared-memory twiddle table");
     }
-    p->p1_smem = gbsp::P1_STAGE_BYTES + (size_t)p->ntab * sizeof(float2);
-    int rc = p1_dispatch(p, true, sms, 0, 0, nullptr, 0, st);
+    int rc = p1_dispatch(p, true, sms, 0, 0, nullptr, 0, nullptr, st);
     if (rc) return rc;
 
     // ---- row-kernel configuration
     p->rows_smem = rows_smem_bytes(p->fd);
-    if (p->K == 1) {
-        GB_CUDA(cudaFuncSetAttribute(gbsp::k_bluestein_rows<false>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->rows_smem));
-        int nb = 0;
-        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gbsp::k_bluestein_rows<false>,
-                                                              gbsp::ROWS_THREADS, p->rows_smem));
-        if (nb < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row kernel does not fit on an SM");
-        p->rows_grid = nb * sms;
-    } else {
-        GB_CUDA(cudaFuncSetAttribute(gbsp::k_bluestein_rows<true>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->rows_smem));
-        cudaLaunchConfig_t cfg = {};
-        cudaLaunchAttribute attr[1];
-        cfg.gridDim = dim3(p->K * sms);
-        cfg.blockDim = dim3(gbsp::ROWS_THREADS);
-        cfg.dynamicSmemBytes = p->rows_smem;
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = p->K;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int ncl = 0;
-        GB_CUDA(cudaOccupancyMaxActiveClusters(&ncl, gbsp::k_bluestein_rows<true>, &cfg));
-        if (ncl < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row-kernel cluster does not fit");
-        p->rows_grid = ncl * p->K;
-    }
+    if ((rc = rows_prepare(p, sms))) return rc;
 
-    // ---- slots: active columns sorted by degree (descending, stable)
+    // ---- CSC upload (rows in column order) and the pass-1 task tables: each
+    // window's nonzeros cut into at most cw + P1_WARPS balanced tasks
     const int na = p->n_active;
-    std::vector<int> order(na);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return (col_ptr[a + 1] - col_ptr[a]) > (col_ptr[b + 1] - col_ptr[b]);
-    });
-    std::vector<int> slot_ptr(na + 1, 0);
-    p->slot_col_host.resize(na);
-    std::vector<uint32_t> rows32(std::max(p->nnz, 1));
-    for (int s = 0; s < na; s++) {
-        const int j = order[s];
-        p->slot_col_host[s] = sparse_cols[j];
-        int w = slot_ptr[s];
-        for (int e = col_ptr[j]; e < col_ptr[j + 1]; e++) rows32[w++] = (uint32_t)row_idx[e];
-        slot_ptr[s + 1] = w;
+    std::vector<int> colp(p->cols + 1, 0);
+    for (int j = 0; j < na; j++) colp[sparse_cols[j] + 1] = col_ptr[j + 1] - col_ptr[j];
+    for (int c = 0; c < p->cols; c++) colp[c + 1] += colp[c];
+    p->s_cols = (p->cols + 1) & ~1;
+    const int CW = p->p1_cw, VM = gbsp::p1_vmax(p->p1_cw);
+    const int n_win = (p->s_cols + CW - 1) / CW;
+    std::vector<uint8_t> slot0((size_t)n_win * (CW + 1));
+    std::vector<int2> task((size_t)n_win * VM, make_int2(0, 0));
+    std::vector<uint8_t> task_col((size_t)n_win * VM, 0);
+    for (int w = 0; w < n_win; w++) {
+        auto deg = [&](int lc) {
+            const int c = w * CW + lc;
+            return c < p->cols ? colp[c + 1] - colp[c] : 0;
+        };
+        long sum = 0;
+        for (int lc = 0; lc < CW; lc++) sum += deg(lc);
+        const long T = std::max<long>(32, (sum + gbsp::P1_WARPS - 1) / gbsp::P1_WARPS);
+        struct Task { int b, e, col; };
+        std::vector<Task> ts;
+        for (int lc = 0; lc < CW; lc++) {
+            slot0[(size_t)w * (CW + 1) + lc] = (uint8_t)ts.size();
+            const int d = deg(lc);
+            if (d == 0) continue;
+            const int np = (int)((d + T - 1) / T);
+            const int base = colp[w * CW + lc];
+            for (int k = 0; k < np; k++)
+                ts.push_back({base + (int)((long)k * d / np), base + (int)((long)(k + 1) * d / np), (int)ts.size()});
+        }
+        if ((int)ts.size() > VM) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 window task overflow");
+        slot0[(size_t)w * (CW + 1) + CW] = (uint8_t)ts.size();
+        std::stable_sort(ts.begin(), ts.end(), [](const Task& a, const Task& b) { return a.e - a.b > b.e - b.b; });
+        for (size_t i = 0; i < ts.size(); i++) {
+            task[(size_t)w * VM + i] = make_int2(ts[i].b, ts[i].e);
+            task_col[(size_t)w * VM + i] = (uint8_t)ts[i].col;
+        }
     }
-    if ((rc = dev_alloc(p, (void**)&p->d_slot_ptr, (size_t)(na + 1) * sizeof(int)))) return rc;
-    if ((rc = dev_alloc(p, (void**)&p->d_slot_col, (size_t)std::max(na, 1) * sizeof(int)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_win_slot0, slot0.size()))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_win_task, task.size() * sizeof(int2)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_win_task_col, task_col.size()))) return rc;
     if ((rc = dev_alloc(p, &p->d_row_idx, (size_t)std::max(p->nnz, 1) * p->idx_bytes))) return rc;
-    GB_CUDA(cudaMemcpyAsync(p->d_slot_ptr, slot_ptr.data(), (size_t)(na + 1) * sizeof(int),
-                            cudaMemcpyHostToDevice, st));
-    if (na > 0)
-        GB_CUDA(cudaMemcpyAsync(p->d_slot_col, p->slot_col_host.data(), (size_t)na * sizeof(int),
-                                cudaMemcpyHostToDevice, st));
+    if ((rc = dev_alloc(p, (void**)&p->d_err, sizeof(int)))) return rc;
+    GB_CUDA(cudaMemsetAsync(p->d_err, 0, sizeof(int), st));
+    GB_CUDA(cudaMemcpyAsync(p->d_win_slot0, slot0.data(), slot0.size(), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(p->d_win_task, task.data(), task.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(p->d_win_task_col, task_col.data(), task_col.size(), cudaMemcpyHostToDevice, st));
     std::vector<uint16_t> r16;
     if (p->nnz > 0) {
         if (p->idx_bytes == 2) {
             r16.resize(p->nnz);
-            for (int i = 0; i < p->nnz; i++) r16[i] = (uint16_t)rows32[i];
+            for (int i = 0; i < p->nnz; i++) r16[i] = (uint16_t)row_idx[i];
             GB_CUDA(cudaMemcpyAsync(p->d_row_idx, r16.data(), (size_t)p->nnz * 2,
                                     cudaMemcpyHostToDevice, st));
         } else {
-            GB_CUDA(cudaMemcpyAsync(p->d_row_idx, rows32.data(), (size_t)p->nnz * 4,
+            GB_CUDA(cudaMemcpyAsync(p->d_row_idx, row_idx, (size_t)p->nnz * 4,
                                     cudaMemcpyHostToDevice, st));
         }
     }
@@ -348,7 +512,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     // ---- tables (FP64 on the device, rounded to FP32)
     const int K = p->K, Lp = p->Lp, cols = p->cols;
     if ((rc = dev_alloc(p, (void**)&p->d_rowtab, (size_t)p->ntab * sizeof(float2)))) return rc;
-    if ((rc = dev_alloc(p, (void**)&p->d_pre, (size_t)K * std::max(na, 1) * sizeof(float2)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&p->d_pre, (size_t)K * cols * sizeof(float2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_post, (size_t)K * cols * sizeof(float2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_filt, (size_t)K * Lp * sizeof(float2)))) return rc;
     const int ntw = std::max(fft_tw_count(p->fd), 1);
@@ -356,11 +520,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
 
     gbsp::k_table_rows<<<blocks_for(p->ntab, 256), 256, 0, st>>>(p->d_rowtab, p->ntab, p->rows);
     GB_CUDA(cudaGetLastError());
-    if (na > 0) {
-        gbsp::k_table_pre<<<blocks_for((long)K * na, 256), 256, 0, st>>>(p->d_pre, p->d_slot_col, na,
-                                                                          cols, p->L, K);
-        GB_CUDA(cudaGetLastError());
-    }
+    gbsp::k_table_pre<<<blocks_for((long)K * cols, 256), 256, 0, st>>>(p->d_pre, cols, p->L, K);
+    GB_CUDA(cudaGetLastError());
     gbsp::k_table_post<<<blocks_for((long)K * cols, 256), 256, 0, st>>>(p->d_post, cols, p->L, K);
     GB_CUDA(cudaGetLastError());
     for (int s = 0; s < p->fd.nst; s++) {
@@ -390,8 +551,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         return set_error(GBSP_ERR_CUDA, std::string("plan tables: ") + cudaGetErrorString(e));
 
     // ---- pass-1 scratch tile
-    p->s_pitch = (size_t)std::max(na, 1);
-    p->s_pitch = (p->s_pitch + 1) & ~(size_t)1;
+    // rows start on 128-byte boundaries; the bulk copy needs 16
+    p->s_pitch = ((size_t)p->s_cols + 15) & ~(size_t)15;
     if ((rc = dev_alloc(p, (void**)&p->d_S, (size_t)p->u_tile * p->s_pitch * sizeof(float2)))) return rc;
     return GBSP_OK;
 }
@@ -449,14 +610,17 @@ int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
     info->u_tile = p->u_tile;
     info->index_bytes = p->idx_bytes;
     info->row_table_mode = p->tab_half;
+    info->rows_threads = p->rows_threads;
     info->device_bytes = p->device_bytes;
     return GBSP_OK;
 }
 
-int gbsp_plan_slot_columns(gbsp_plan_t p, int* cols_out) {
-    if (!p || (!cols_out && p->n_active > 0))
-        return set_error(GBSP_ERR_INVALID, "gbsp_plan_slot_columns: null argument");
-    std::copy(p->slot_col_host.begin(), p->slot_col_host.end(), cols_out);
+int gbsp_plan_error_flags(gbsp_plan_t p, int* flags) {
+    if (!p || !flags) return set_error(GBSP_ERR_INVALID, "gbsp_plan_error_flags: null argument");
+    int f = 0;
+    GB_CUDA(cudaMemcpy(&f, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+    *flags = f;
     return GBSP_OK;
 }
 
@@ -471,7 +635,7 @@ int gbsp_execute(gbsp_plan_t p, void* d_out, size_t out_pitch, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     for (int u0 = 0; u0 < p->half_rows; u0 += p->u_tile) {
         const int n = std::min(p->u_tile, p->half_rows - u0);
-        if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, st))) return rc;
+        if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p->d_post, st))) return rc;
         if ((rc = launch_rows(p, u0, n, d_out, out_pitch, st))) return rc;
     }
     return GBSP_OK;
@@ -492,7 +656,7 @@ int gbsp_execute_profiled(gbsp_plan_t p, void* d_out, size_t out_pitch, void* st
     for (int t = 0; t < ntiles && rc == GBSP_OK; t++) {
         const int u0 = t * p->u_tile;
         const int n = std::min(p->u_tile, p->half_rows - u0);
-        rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, st);
+        rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p->d_post, st);
         if (rc == GBSP_OK && cudaEventRecord(ev[2 * t + 1], st) != cudaSuccess) rc = GBSP_ERR_CUDA;
         if (rc == GBSP_OK) rc = launch_rows(p, u0, n, d_out, out_pitch, st);
         if (rc == GBSP_OK && cudaEventRecord(ev[2 * t + 2], st) != cudaSuccess) rc = GBSP_ERR_CUDA;
@@ -509,6 +673,9 @@ int gbsp_execute_profiled(gbsp_plan_t p, void* d_out, size_t out_pitch, void* st
     for (auto e : ev)
         if (e) cudaEventDestroy(e);
     if (rc != GBSP_OK) return set_error(rc, "gbsp_execute_profiled: CUDA failure");
+    int flags = 0;
+    GB_CUDA(cudaMemcpy(&flags, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flags) return set_error(GBSP_ERR_CUDA, "gbsp_execute_profiled: a bounded device wait timed out");
     *ms_pass1 = a;
     *ms_rows = b;
     return GBSP_OK;
@@ -516,9 +683,9 @@ int gbsp_execute_profiled(gbsp_plan_t p, void* d_out, size_t out_pitch, void* st
 
 int gbsp_column_sums(gbsp_plan_t p, int u0, int n_rows, void* d_s, size_t s_pitch, void* stream) {
     if (!p || !d_s) return set_error(GBSP_ERR_INVALID, "gbsp_column_sums: null argument");
-    if (u0 < 0 || n_rows < 1 || u0 + n_rows > p->rows || s_pitch < (size_t)std::max(p->n_active, 1))
-        return set_error(GBSP_ERR_INVALID, "gbsp_column_sums: bad range or pitch");
-    return launch_pass1(p, u0, n_rows, (float2*)d_s, s_pitch, (cudaStream_t)stream);
+    if (u0 < 0 || n_rows < 1 || u0 + n_rows > p->rows || s_pitch < (size_t)p->s_cols)
+        return set_error(GBSP_ERR_INVALID, "gbsp_column_sums: bad range or pitch (>= cols rounded up to even)");
+    return launch_pass1(p, u0, n_rows, (float2*)d_s, s_pitch, nullptr, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -108,14 +108,18 @@ class Plan:
 
     def __init__(self, coo: COOMatrix, *, length_policy: int = GBSP_LEN_3SMOOTH, u_tile: int = 0,
                  kahan_min_degree: int = 0, index_bytes: int = 0, max_channel_len: int = 0,
-                 stream=None, csc: Optional[CompactCSC] = None):
+                 rows_threads: int = 0, row_table_mode: int = 0, radix=None, stream=None,
+                 csc: Optional[CompactCSC] = None):
         lib = load()
         self._lib = lib
         self._h = C.c_void_p()
         csc = csc if csc is not None else make_compact_csc(coo)
         self.rows, self.cols = coo.rows, coo.cols
         o = GbspOptions(length_policy=length_policy, u_tile=u_tile, kahan_min_degree=kahan_min_degree,
-                        index_bytes=index_bytes, max_channel_len=max_channel_len)
+                        index_bytes=index_bytes, max_channel_len=max_channel_len,
+                        rows_threads=rows_threads, row_table_mode=row_table_mode)
+        for i, r in enumerate(radix or ()):
+            o.radix[i] = int(r)
         cp = np.ascontiguousarray(csc.col_ptr, np.int32)
         ri = np.ascontiguousarray(csc.row_idx if coo.nnz else np.zeros(1, np.int32), np.int32)
         sc = np.ascontiguousarray(csc.sparse_cols if csc.n_sparse_cols else np.zeros(1, np.int32),
@@ -151,15 +155,14 @@ class Plan:
               "gbsp_execute_profiled")
         return a.value, b.value
 
-    def slot_columns(self) -> np.ndarray:
-        """Column index of each pass-1 slot (active columns by decreasing degree)."""
-        n = self.info["n_active"]
-        cols = np.zeros(max(n, 1), np.int32)
-        check(self._lib.gbsp_plan_slot_columns(self._h, _ip(cols)), "gbsp_plan_slot_columns")
-        return cols[:n]
+    def error_flags(self) -> int:
+        """Reads and clears the device error word (0 = no bounded wait timed out)."""
+        f = C.c_int()
+        check(self._lib.gbsp_plan_error_flags(self._h, C.byref(f)), "gbsp_plan_error_flags")
+        return f.value
 
     def column_sums(self, u0: int, n_rows: int, out, stream=None) -> None:
-        """S[u-u0][slot] for u in [u0, u0+n_rows); slots ordered as slot_columns()."""
+        """S[u-u0][c] for u in [u0, u0+n_rows) and every column c (pitch >= cols rounded up to even)."""
         check(self._lib.gbsp_column_sums(self._h, u0, n_rows, C.c_void_p(out.data_ptr()), out.shape[1],
                                          _stream_handle(stream)), "gbsp_column_sums")
 

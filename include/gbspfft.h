@@ -58,8 +58,14 @@ typedef struct {
     int max_channel_len;   /* largest per-CTA FFT length held in shared memory;
                               0 = default; longer convolutions split into channels that
                               run as one thread-block cluster                             */
-    int reserved0;         /* must be 0                                                  */
-    int reserved[8];
+    int rows_threads;      /* row-kernel block size: 0 = auto, else a multiple of 32
+                              in [64, 1024] (at most 512 when a radix exceeds 16)         */
+    int row_table_mode;    /* pass-1 twiddle table: 0 = auto, 1 = full circle,
+                              2 = half circle (smaller, more blocks per SM)               */
+    int radix[8];          /* channel FFT radix per stage, first to last, 0-terminated;
+                              all zero = auto.  Allowed: 2 3 4 5 7 8 9 12 15 16 20 21
+                              24 25 28 32 35 40; product = channel length                 */
+    int reserved[4];
 } gbsp_options;
 
 typedef struct {
@@ -76,6 +82,7 @@ typedef struct {
     int u_tile;            /* effective Bluestein rows per tile                           */
     int index_bytes;       /* 2 or 4                                                      */
     int row_table_mode;    /* 0 full twiddle table in shared memory, 1 half table        */
+    int rows_threads;      /* row-kernel block size in use                                */
     size_t device_bytes;   /* device memory held by the plan                              */
 } gbsp_plan_info;
 
@@ -138,17 +145,18 @@ int gbsp_execute_profiled(gbsp_plan_t plan, void* d_out, size_t out_pitch, void*
 
 /* The pass-1 intermediate for inspection and tests: for rows
  * u in [u0, u0+n_rows) (u0+n_rows <= rows) writes
- *   S[u-u0][j] = sum over nonzero rows r of slot j of exp(-2*pi*i*u*r/rows)
- * to d_s (complex64, row pitch s_pitch >= n_active).  Slots are the active
- * columns ordered by decreasing nonzero count; gbsp_plan_slot_columns gives
- * the column of each slot.  This is the reference's
- * csc_build_bluestein_input_*kernel (src/sparse_fft_bluestein.cu:334-397)
- * before its chirp multiply. */
+ *   S[u-u0][c] = sum over nonzero rows r of column c of exp(-2*pi*i*u*r/rows)
+ * for every column c < cols (zero for empty columns) to d_s (complex64, row
+ * pitch s_pitch >= cols rounded up to even; one extra zero column when cols
+ * is odd).  This is the reference's csc_build_bluestein_input_*kernel
+ * (src/sparse_fft_bluestein.cu:334-397) before its chirp multiply. */
 int gbsp_column_sums(gbsp_plan_t plan, int u0, int n_rows, void* d_s, size_t s_pitch,
                      void* stream);
 
-/* Copies the column index of each slot (n_active ints) to host memory. */
-int gbsp_plan_slot_columns(gbsp_plan_t plan, int* cols_out);
+/* Reads and clears the plan's device error flags (synchronises the device).
+ * Bit 0: a bounded wait inside a kernel gave up (the result of that
+ * transform is not valid).  0 means no error was recorded. */
+int gbsp_plan_error_flags(gbsp_plan_t plan, int* flags);
 
 #ifdef __cplusplus
 }

@@ -124,18 +124,15 @@ def test_symmetric_transpose_property(cuda):
 def test_column_sums(cuda):
     import torch
     coo = synthetic.uniform_matrix(211, 77, 2000, seed=5)
-    csc = gb.make_compact_csc(coo)
     with gb.Plan(coo) as plan:
-        slots = plan.slot_columns()
-        s = torch.zeros((150, csc.n_sparse_cols), dtype=torch.complex64, device="cuda")
+        s = torch.zeros((150, 80), dtype=torch.complex64, device="cuda")
         plan.column_sums(30, 150, s)
         torch.cuda.synchronize()
         got = s.cpu().numpy()
-    assert sorted(slots.tolist()) == csc.sparse_cols.tolist()
-    deg = np.diff(csc.col_ptr)[np.searchsorted(csc.sparse_cols, slots)]
-    assert np.all(np.diff(deg) <= 0), "slots must be ordered by decreasing degree"
+        assert plan.error_flags() == 0
     ref = fp64.column_sums_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, np.arange(30, 180))
-    assert fp64.rel_l2(got, ref[:, slots]) < 1e-6
+    assert fp64.rel_l2(got[:, :coo.cols], ref) < 1e-6
+    assert np.all(got[:, coo.cols:78] == 0)
 
 
 def test_config_uniform_3001x2048_full(cuda):
