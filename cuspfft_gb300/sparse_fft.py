@@ -96,8 +96,13 @@ def next_smooth(n: int, policy: int = GBSP_LEN_3SMOOTH) -> int:
 
 
 def _stream_handle(stream) -> Optional[int]:
+    """cudaStream_t of a torch stream; torch's current stream when None (the
+    legacy default stream if CUDA is unavailable -- the library then reports
+    the missing device itself)."""
     import torch
     if stream is None:
+        if not torch.cuda.is_available():
+            return None
         stream = torch.cuda.current_stream()
     return stream.cuda_stream
 

@@ -1,0 +1,65 @@
+"""The C-ABI library loads and exports every entry point its headers
+declare (no GPU needed; nothing here launches a kernel)."""
+import ctypes as C
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+import cuspfft_gb300 as gb
+from cuspfft_gb300 import _capi
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_c_functions():
+    text = (ROOT / "include" / "gbspfft.h").read_text()
+    return sorted(set(re.findall(r"\b(gbsp_\w+)\s*\(", text)))
+
+
+def test_c_symbols_exported():
+    lib = _capi.load()
+    names = declared_c_functions()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(_capi.EXPORTED) == set(names)
+
+
+@pytest.mark.skipif(shutil.which("nm") is None, reason="nm not available")
+def test_cpp_dropin_symbols_exported():
+    out = subprocess.run(["nm", "-DC", "--defined-only", str(_capi.LIB_PATH)], capture_output=True,
+                         text=True, check=True).stdout
+    text = (ROOT / "include" / "sparse_fft.h").read_text() + (ROOT / "include" / "mtx_reader.h").read_text() \
+        + (ROOT / "include" / "sparse_fft_csc.h").read_text()
+    funcs = set(re.findall(r"^\w[\w:<>]*\s+(\w+)\(", text, re.M))
+    assert {"sparse_fft_csc_bluestein_mixed_radix", "sparse_fft_csc_bluestein_cufft_smooth", "read_mtx",
+            "make_compact_csc", "coo_to_csr"} <= funcs
+    for f in funcs:
+        assert re.search(rf"\b{f}\(", out), f"{f} not exported"
+
+
+def test_status_and_errors_without_gpu():
+    lib = _capi.load()
+    assert lib.gbsp_version() > 0
+    assert _capi.status_string(_capi.GBSP_ERR_INVALID) == "invalid argument"
+    # invalid CSC is rejected before any device work
+    cp = (C.c_int * 2)(0, 5)
+    ri = (C.c_int * 1)(0)
+    sc = (C.c_int * 1)(0)
+    h = C.c_void_p()
+    st = lib.gbsp_plan_create(3, 3, 1, 1, cp, ri, sc, None, None, C.byref(h))
+    assert st == _capi.GBSP_ERR_INVALID
+    assert "col_ptr" in _capi.last_error()
+    assert lib.gbsp_next_smooth(16437, 9) == -1
+
+
+def test_plan_create_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    coo = gb.COOMatrix(4, 4, [0, 1], [1, 2])
+    with pytest.raises(gb.GbspError):
+        gb.Plan(coo)
