@@ -264,12 +264,12 @@ def main():
     achieved_gbs = d["bytes"] / (d["ms"] * 1e-3) / 1e9
     achieved_tf = d["flops"] / (d["ms"] * 1e-3) / 1e12
     traffic = None
-    tr_path = ROOT / "profiles" / "traffic.json"
+    tr_path = ROOT / "profiles" / "traffic.txt"
     if tr_path.exists():
-        try:
-            traffic = json.loads(tr_path.read_text()).get(args.workload, {}).get(dom)
-        except ValueError:
-            traffic = None
+        for ln in tr_path.read_text().splitlines():
+            f = ln.split()
+            if len(f) == 3 and not ln.startswith("#") and f[0] == args.workload and f[1] == dom:
+                traffic = int(f[2])
     roofline = {
         "kernel": dom, "bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
         "frac": round(achieved_gbs / hbm_peak, 4), "traffic": traffic,

@@ -151,9 +151,17 @@ __global__ void k_table_filter_input(double2* __restrict__ bq, int cols, int L, 
 // plan for the filter spectrum, so it follows the row kernel's network.
 constexpr int MAX_RADIX = 64;
 __global__ void k_dif_stage_f64(double2* __restrict__ data, int K, int Lp, int R, int m) {
+    __shared__ double2 root[MAX_RADIX];  // W_R^e, e < R
+    if (R > MAX_RADIX) return;
+    for (int e = threadIdx.x; e < R; e += blockDim.x) {
+        double sn, cs;
+        sincospi(-2.0 * (double)e / (double)R, &sn, &cs);
+        root[e] = make_double2(cs, sn);
+    }
+    __syncthreads();
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int nb = Lp / R;
-    if (idx >= (long)K * nb || R > MAX_RADIX) return;
+    if (idx >= (long)K * nb) return;
     int ch = (int)(idx / nb);
     int t = (int)(idx - (long)ch * nb);
     double2* x = data + (size_t)ch * Lp;
@@ -164,11 +172,7 @@ __global__ void k_dif_stage_f64(double2* __restrict__ data, int K, int Lp, int R
     for (int s = 0; s < R; s++) in[s] = x[base + s * m];
     for (int q = 0; q < R; q++) {
         double2 acc = make_double2(0.0, 0.0);
-        for (int s = 0; s < R; s++) {
-            double sn, cs;
-            sincospi(-2.0 * (double)((s * q) % R) / (double)R, &sn, &cs);
-            acc = cadd(acc, cmul(in[s], make_double2(cs, sn)));
-        }
+        for (int s = 0, e = 0; s < R; s++, e = (e + q) % R) acc = cadd(acc, cmul(in[s], root[e]));
         long long e = ((long long)q * k * l) % Lp;
         double sn, cs;
         sincospi(-2.0 * (double)e / (double)Lp, &sn, &cs);

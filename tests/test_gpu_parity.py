@@ -164,3 +164,50 @@ def test_reference_api_methods(cuda):
         assert fp64.rel_l2(got, ref) < REL_L2_TOL
     with pytest.raises(RuntimeError):
         gb.sparse_fft_csc_bluestein_mixed_radix(coo, 0)
+
+
+@pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH])
+@pytest.mark.parametrize("shape", [(64, 64, 400), (101, 127, 900), (300, 257, 3000), (211, 1000, 4000)])
+def test_against_reference_gpu_method_port(cuda, policy, shape):
+    # the FP32 restatement of the reference's own method on the same input:
+    # rel-L2 <= 1e-5 between the two FP32 forms
+    from oracle import ref_port
+    g = np.random.default_rng(shape[0] + shape[1])
+    coo = synthetic.normalise(shape[0], shape[1], g.integers(0, shape[0], shape[2]),
+                              g.integers(0, shape[1], shape[2]))
+    got, _ = run_plan(coo, length_policy=policy)
+    port = ref_port.reference_gpu_method(coo.rows, coo.cols, coo.row_idx, coo.col_idx, policy)
+    assert fp64.rel_l2(got[:, : coo.cols // 2 + 1], port) <= REL_L2_TOL
+
+
+def test_uniform_3001x2048_vs_reference_port(cuda):
+    from oracle import ref_port
+    coo = synthetic.config_matrix("uniform_3001x2048")
+    got, _ = run_plan(coo, length_policy=gb.GBSP_LEN_3SMOOTH)
+    port = ref_port.reference_gpu_method(coo.rows, coo.cols, coo.row_idx, coo.col_idx, 3)
+    assert fp64.rel_l2(got[:, : coo.cols // 2 + 1], port) <= REL_L2_TOL
+
+
+def test_cli_methods_with_host_reference(cuda, tmp_path):
+    # the reference-compatible driver end to end: read .mtx, run both hot
+    # methods and the graph replay, check lines against the FP64 host spectrum
+    import subprocess
+    from cuspfft_gb300 import build
+    coo = synthetic.uniform_matrix(97, 130, 900, seed=31)
+    path = tmp_path / "m.mtx"
+    with open(path, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate pattern general\n")
+        f.write(f"{coo.rows} {coo.cols} {coo.nnz}\n")
+        for r, c in zip(coo.row_idx, coo.col_idx):
+            f.write(f"{r + 1} {c + 1}\n")
+    exe = build.build().parent / "cuspfft_gb300"
+    res = subprocess.run([str(exe), str(path), "--sparse-only", "--cpu-reference", "--csc-mixed-radix",
+                          "--csc-cufft-smooth", "--csc-mixed-radix-graph", "--csc-tile", "16", "--repeat", "3"],
+                         capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    checks = [ln for ln in res.stdout.splitlines() if ln.strip().startswith("check")]
+    assert len(checks) == 3, res.stdout
+    for ln in checks:
+        max_rel = float(ln.split("max_rel")[1].split()[0])
+        assert max_rel < 1e-4, ln
+    assert "n=3" in res.stdout
