@@ -28,7 +28,7 @@ EXPORTED = (
     "gbsp_version", "gbsp_status_string", "gbsp_last_error", "gbsp_read_mtx", "gbsp_free",
     "gbsp_build_compact_csc", "gbsp_next_smooth", "gbsp_plan_create", "gbsp_plan_get_info",
     "gbsp_plan_destroy", "gbsp_execute", "gbsp_execute_profiled", "gbsp_column_sums",
-    "gbsp_plan_error_flags",
+    "gbsp_plan_error_flags", "gbsp_execute_noalloc",
 )
 
 
@@ -101,6 +101,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                            C.POINTER(C.c_float)]
     lib.gbsp_column_sums.argtypes = [vp, i32, i32, vp, C.c_size_t, vp]
     lib.gbsp_plan_error_flags.argtypes = [vp, ip]
+    lib.gbsp_execute_noalloc.argtypes = [vp, vp, C.c_size_t, vp]
     for name in EXPORTED:
         if name not in ("gbsp_status_string", "gbsp_free"):
             getattr(lib, name).restype = i32

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -689,3 +690,95 @@ int gbsp_column_sums(gbsp_plan_t p, int u0, int n_rows, void* d_s, size_t s_pitc
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free execution.
+//
+// Some callers must not allocate device memory when they run a transform:
+// code whose device memory is owned by a pool with a hard budget (a
+// framework's caching allocator that forbids side allocations), latency-
+// critical loops where cudaMalloc's implicit synchronisation is not
+// acceptable, or code paths that only enqueue work.  For them
+// gbsp_execute_noalloc runs the same two kernels as gbsp_execute, but the
+// pass-1 intermediate (the S tile the row kernel reads) lives in a fixed
+// array compiled into this library instead of a per-plan allocation; it
+// calls no allocating routine.  The array is 32 MiB and every GPU that loads
+// the library holds it until the process exits.
+// ===========================================================================
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)32 << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch on each device, looked up once per
+// device (with that device current) on that device's first call.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+int noalloc_scratch_address(int device, void** addr) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_execute_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return set_error(GBSP_ERR_CUDA, std::string("gbsp_execute_noalloc: cudaGetSymbolAddress: ") +
+                                                cudaGetErrorString(e));
+        g_noalloc_addr[device] = ptr;
+    }
+    *addr = g_noalloc_addr[device];
+    return GBSP_OK;
+}
+
+// the row kernel reading its input rows from an explicit S tile
+template <bool CL, int NTMAX>
+int rows_launch_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
+                     size_t out_pitch, cudaStream_t st) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>, S, s_pitch, (const float2*)p->d_pre,
+                               (const float2*)p->d_post, (const float2*)p->d_filt, (const float2*)p->d_fftw,
+                               p->fd, p->K, p->rows, p->cols, u0, n, (float2*)d_out, out_pitch, p->d_err));
+    return GBSP_OK;
+}
+
+int launch_rows_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
+                     size_t out_pitch, cudaStream_t st) {
+    if (p->K == 1)
+        return p->rows_ntmax == 512 ? rows_launch_from<false, 512>(p, S, s_pitch, u0, n, d_out, out_pitch, st)
+                                    : rows_launch_from<false, 1024>(p, S, s_pitch, u0, n, d_out, out_pitch, st);
+    return p->rows_ntmax == 512 ? rows_launch_from<true, 512>(p, S, s_pitch, u0, n, d_out, out_pitch, st)
+                                : rows_launch_from<true, 1024>(p, S, s_pitch, u0, n, d_out, out_pitch, st);
+}
+
+}  // namespace
+
+extern "C" int gbsp_execute_noalloc(gbsp_plan_t p, void* d_out, size_t out_pitch, void* stream) {
+    int rc = check_out(p, d_out, out_pitch, "gbsp_execute_noalloc");
+    if (rc) return rc;
+    int dev = -1;
+    GB_CUDA(cudaGetDevice(&dev));
+    if (dev != p->device)
+        return set_error(GBSP_ERR_INVALID, "gbsp_execute_noalloc: the plan's device must be current");
+    const size_t row_bytes = p->s_pitch * sizeof(float2);
+    if (row_bytes > NOALLOC_SCRATCH_BYTES)
+        return set_error(GBSP_ERR_UNSUPPORTED,
+                         "gbsp_execute_noalloc: one pass-1 row needs " + std::to_string(row_bytes) +
+                             " bytes, more than the fixed scratch array (" +
+                             std::to_string(NOALLOC_SCRATCH_BYTES) + " bytes)");
+    void* scratch = nullptr;
+    if ((rc = noalloc_scratch_address(dev, &scratch))) return rc;
+    // Tiles sized to the array.  Nothing in it has to start at zero: pass 1
+    // writes every element of a tile row that the row kernel reads.
+    const int tile = (int)std::min<size_t>((size_t)p->u_tile, NOALLOC_SCRATCH_BYTES / row_bytes);
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int u0 = 0; u0 < p->half_rows; u0 += tile) {
+        const int n = std::min(tile, p->half_rows - u0);
+        if ((rc = launch_pass1(p, u0, n, (float2*)scratch, p->s_pitch, p->d_post, st))) return rc;
+        if ((rc = launch_rows_from(p, (const float2*)scratch, p->s_pitch, u0, n, d_out, out_pitch, st)))
+            return rc;
+    }
+    return GBSP_OK;
+}

@@ -153,6 +153,28 @@ int gbsp_execute_profiled(gbsp_plan_t plan, void* d_out, size_t out_pitch, void*
 int gbsp_column_sums(gbsp_plan_t plan, int u0, int n_rows, void* d_s, size_t s_pitch,
                      void* stream);
 
+/* Allocation-free variant of gbsp_execute (this entry point has no
+ * counterpart in the reference).  For callers that must not allocate device
+ * memory while they run transforms -- device memory owned by a pool with a
+ * hard budget, or latency-critical code that cannot afford cudaMalloc's
+ * implicit synchronisation: it computes the same result as gbsp_execute, but
+ * the pass-1 intermediate lives in a fixed 32 MiB array inside the library
+ * (held by every GPU that loads the library until the process exits) and no
+ * allocating routine is called.
+ *   - The plan's device must be current.  The first call on each device looks
+ *     up the array's device address; make that first call before any stream
+ *     capture.
+ *   - Rows of the intermediate are processed in tiles that fit the array; a
+ *     plan whose single row would not fit is rejected with
+ *     GBSP_ERR_UNSUPPORTED (cannot happen for plans gbsp_plan_create accepts
+ *     today: a row is at most a few hundred KB).
+ *   - All calls share the array and nothing in it has to start at zero (each
+ *     tile is fully rewritten before it is read).  Calls that overlap on the
+ *     GPU -- concurrent streams, or several host threads -- race on it:
+ *     serialise them.
+ * Asynchronous on `stream`, like gbsp_execute. */
+int gbsp_execute_noalloc(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream);
+
 /* Reads and clears the plan's device error flags (synchronises the device).
  * Bit 0: a bounded wait inside a kernel gave up (the result of that
  * transform is not valid).  0 means no error was recorded. */
