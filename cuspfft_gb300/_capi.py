@@ -28,7 +28,9 @@ EXPORTED = (
     "gbsp_version", "gbsp_status_string", "gbsp_last_error", "gbsp_read_mtx", "gbsp_free",
     "gbsp_build_compact_csc", "gbsp_next_smooth", "gbsp_plan_create", "gbsp_plan_get_info",
     "gbsp_plan_destroy", "gbsp_execute", "gbsp_execute_profiled", "gbsp_column_sums",
-    "gbsp_plan_error_flags", "gbsp_execute_noalloc",
+    "gbsp_plan_error_flags", "gbsp_execute_noalloc", "gbsp_batch_create", "gbsp_batch_set_outputs",
+    "gbsp_batch_execute", "gbsp_batch_graph_launch", "gbsp_batch_plan_info", "gbsp_batch_error_flags",
+    "gbsp_batch_destroy",
 )
 
 
@@ -60,6 +62,14 @@ class GbspPlanInfo(C.Structure):
         d = {name: getattr(self, name) for name, _ in self._fields_ if name != "radix"}
         d["radix"] = [self.radix[i] for i in range(self.n_stages)]
         return d
+
+
+class GbspMatrix(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int), ("cols", C.c_int), ("n_active", C.c_int), ("nnz", C.c_int),
+        ("col_ptr", C.POINTER(C.c_int)), ("row_idx", C.POINTER(C.c_int)),
+        ("sparse_cols", C.POINTER(C.c_int)),
+    ]
 
 
 class GbspError(RuntimeError):
@@ -102,6 +112,13 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbsp_column_sums.argtypes = [vp, i32, i32, vp, C.c_size_t, vp]
     lib.gbsp_plan_error_flags.argtypes = [vp, ip]
     lib.gbsp_execute_noalloc.argtypes = [vp, vp, C.c_size_t, vp]
+    lib.gbsp_batch_create.argtypes = [i32, C.POINTER(GbspMatrix), C.POINTER(GbspOptions), vp, C.POINTER(vp)]
+    lib.gbsp_batch_set_outputs.argtypes = [vp, C.POINTER(vp), C.POINTER(C.c_size_t)]
+    lib.gbsp_batch_execute.argtypes = [vp, vp]
+    lib.gbsp_batch_graph_launch.argtypes = [vp, vp]
+    lib.gbsp_batch_plan_info.argtypes = [vp, i32, C.POINTER(GbspPlanInfo)]
+    lib.gbsp_batch_error_flags.argtypes = [vp, ip]
+    lib.gbsp_batch_destroy.argtypes = [vp]
     for name in EXPORTED:
         if name not in ("gbsp_status_string", "gbsp_free"):
             getattr(lib, name).restype = i32

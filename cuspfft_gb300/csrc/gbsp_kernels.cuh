@@ -347,91 +347,160 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
     }
 }
 
+// One matrix's pass-1 inputs for one tile of Bluestein rows [u0, u0+tile_rows).
 // win_slot0[w*(cw+1) + lc]: first tile column of window w's column lc
 // (entry cw = tasks in the window); win_task[w*vmax + i] = nonzero range
 // (begin, end) and win_task_col[...] its tile column, longest task first.
 // S row u-u0 gets columns [0, s_cols), zero past cols.
-template <typename IDX, bool TAB_HALF, bool BIG, int KU>
-__global__ void __launch_bounds__(P1_THREADS, 1)
-k_twiddle_sum(const IDX* __restrict__ row_idx, const uint8_t* __restrict__ win_slot0,
-              const int2* __restrict__ win_task, const uint8_t* __restrict__ win_task_col, int cw,
-              int cols, int s_cols, const float2* __restrict__ row_tab, int ntab, int rows, uint32_t magic,
-              const float2* __restrict__ chirp, int u0, int tile_rows, float2* __restrict__ S,
-              size_t s_pitch, int kahan_min) {
-    constexpr int UBLK = 32 * KU;
-    extern __shared__ float4 smem_raw[];
-    const int pitch = p1_pitch(cw), vmax = p1_vmax(cw);
-    float2* stage = reinterpret_cast<float2*>(smem_raw);
-    NzInfo* info_all = reinterpret_cast<NzInfo*>(stage + (size_t)UBLK * pitch);
-    float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
-    __shared__ int next_task;
-    __shared__ int s_slot0[64 + 1];
-    __shared__ float2 s_chirp[64];
-    for (int i = threadIdx.x; i < ntab; i += blockDim.x) tab[i] = row_tab[i];
-    if (threadIdx.x == 0) next_task = 0;
-    __syncthreads();
+struct P1Args {
+    const void* row_idx;
+    const uint8_t* win_slot0;
+    const int2* win_task;
+    const uint8_t* win_task_col;
+    const float2* row_tab;
+    const float2* chirp;  // nullptr: raw column sums
+    float2* S;
+    size_t s_pitch;
+    int cw, cols, s_cols, ntab, rows, u0, tile_rows, kahan_min;
+    uint32_t magic;
+};
 
+struct P1Shared {
+    int next_task;
+    int slot0[64 + 1];
+    float2 chirp[64];
+};
+
+__device__ __forceinline__ long p1_items(const P1Args& a, int ublk) {
+    return (long)((a.tile_rows + ublk - 1) / ublk) * ((a.s_cols + a.cw - 1) / a.cw);
+}
+
+// Work item `it` of one matrix: all tasks of one (row block, column window),
+// then the window's tile written to S.  Whole CTA; tab holds the matrix's
+// twiddle table.
+template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+__device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage, NzInfo* info_all,
+                                        const float2* tab, P1Shared& sh) {
+    constexpr int UBLK = 32 * KU;
+    const int pitch = p1_pitch(a.cw), vmax = p1_vmax(a.cw), cw = a.cw;
     const int lane = threadIdx.x & 31;
     NzInfo* info = info_all + (threadIdx.x >> 5) * 32;
-    const int n_ublk = (tile_rows + UBLK - 1) / UBLK;
-    const int n_win = (s_cols + cw - 1) / cw;
-    const long nitems = (long)n_ublk * n_win;
-
-    for (long it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int ub = (int)(it / n_win);
-        const int w = (int)(it - (long)ub * n_win);
-        const int ul0 = ub * UBLK;
-        const int c0 = w * cw;
-        const uint8_t* slot0 = win_slot0 + (size_t)w * (cw + 1);
-        if (threadIdx.x <= cw) s_slot0[threadIdx.x] = slot0[threadIdx.x];
-        if (threadIdx.x < cw) {
-            const int c = c0 + threadIdx.x;
-            s_chirp[threadIdx.x] = (chirp && c < cols) ? chirp[c] : make_float2(1.f, 0.f);
-        }
-        const int ntask = slot0[cw];
-        const uint32_t u_lane = (uint32_t)(u0 + ul0 + lane) % (uint32_t)rows;
-        for (;;) {
-            int i = 0;
-            if (lane == 0) i = atomicAdd(&next_task, 1);
-            i = __shfl_sync(0xffffffffu, i, 0);
-            if (i >= ntask) break;
-            const int2 range = win_task[(size_t)w * vmax + i];
-            const int col = win_task_col[(size_t)w * vmax + i];
-            float2 acc[KU];
-            column_sums_warp<IDX, TAB_HALF, BIG, KU>(row_idx, range.x, range.y, tab, info, u_lane,
-                                                     (uint32_t)rows, magic, lane,
-                                                     kahan_min > 0 && range.y - range.x >= kahan_min, acc);
+    const int n_win = (a.s_cols + cw - 1) / cw;
+    const int ub = (int)(it / n_win);
+    const int w = (int)(it - (long)ub * n_win);
+    const int ul0 = ub * UBLK;
+    const int c0 = w * cw;
+    const uint8_t* slot0 = a.win_slot0 + (size_t)w * (cw + 1);
+    if (threadIdx.x <= cw) sh.slot0[threadIdx.x] = slot0[threadIdx.x];
+    if (threadIdx.x < cw) {
+        const int c = c0 + threadIdx.x;
+        sh.chirp[threadIdx.x] = (a.chirp && c < a.cols) ? a.chirp[c] : make_float2(1.f, 0.f);
+    }
+    const int ntask = slot0[cw];
+    const uint32_t u_lane = (uint32_t)(a.u0 + ul0 + lane) % (uint32_t)a.rows;
+    const IDX* row_idx = static_cast<const IDX*>(a.row_idx);
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(&sh.next_task, 1);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= ntask) break;
+        const int2 range = a.win_task[(size_t)w * vmax + i];
+        const int col = a.win_task_col[(size_t)w * vmax + i];
+        float2 acc[KU];
+        column_sums_warp<IDX, TAB_HALF, BIG, KU>(row_idx, range.x, range.y, tab, info, u_lane,
+                                                 (uint32_t)a.rows, a.magic, lane,
+                                                 a.kahan_min > 0 && range.y - range.x >= a.kahan_min, acc);
 #pragma unroll
-            for (int kk = 0; kk < KU; kk++) stage[(lane + 32 * kk) * pitch + col] = acc[kk];
-        }
-        __syncthreads();
-        const int ncol = min(cw, s_cols - c0);
-        for (int e = threadIdx.x; e < UBLK * cw; e += blockDim.x) {
-            const int row = e / cw, lc = e - (e / cw) * cw;
-            const int ul = ul0 + row;
-            if (ul >= tile_rows || lc >= ncol) continue;
-            const int a = s_slot0[lc], b = s_slot0[lc + 1];
-            const float2* srow = stage + row * pitch;
-            float2 v = make_float2(0.f, 0.f);
-            if (b - a == 1) {
-                v = srow[a];
-            } else {
-                float2 comp = make_float2(0.f, 0.f);
-                for (int k = a; k < b; k++) {  // parts in a fixed order, compensated
-                    float y = srow[k].x - comp.x;
-                    float t = v.x + y;
-                    comp.x = (t - v.x) - y;
-                    v.x = t;
-                    y = srow[k].y - comp.y;
-                    t = v.y + y;
-                    comp.y = (t - v.y) - y;
-                    v.y = t;
-                }
+        for (int kk = 0; kk < KU; kk++) stage[(lane + 32 * kk) * pitch + col] = acc[kk];
+    }
+    __syncthreads();
+    const int ncol = min(cw, a.s_cols - c0);
+    for (int e = threadIdx.x; e < UBLK * cw; e += blockDim.x) {
+        const int row = e / cw, lc = e - (e / cw) * cw;
+        const int ul = ul0 + row;
+        if (ul >= a.tile_rows || lc >= ncol) continue;
+        const int p0 = sh.slot0[lc], p1 = sh.slot0[lc + 1];
+        const float2* srow = stage + row * pitch;
+        float2 v = make_float2(0.f, 0.f);
+        if (p1 - p0 == 1) {
+            v = srow[p0];
+        } else {
+            float2 comp = make_float2(0.f, 0.f);
+            for (int k = p0; k < p1; k++) {  // parts in a fixed order, compensated
+                float y = srow[k].x - comp.x;
+                float t = v.x + y;
+                comp.x = (t - v.x) - y;
+                v.x = t;
+                y = srow[k].y - comp.y;
+                t = v.y + y;
+                comp.y = (t - v.y) - y;
+                v.y = t;
             }
-            S[(size_t)ul * s_pitch + c0 + lc] = cmul(v, s_chirp[lc]);
         }
-        if (threadIdx.x == 0) next_task = 0;
+        a.S[(size_t)ul * a.s_pitch + c0 + lc] = cmul(v, sh.chirp[lc]);
+    }
+    if (threadIdx.x == 0) sh.next_task = 0;
+    __syncthreads();
+}
+
+template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+__global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
+    extern __shared__ float4 smem_raw[];
+    __shared__ P1Shared sh;
+    float2* stage = reinterpret_cast<float2*>(smem_raw);
+    NzInfo* info_all = reinterpret_cast<NzInfo*>(stage + (size_t)32 * KU * p1_pitch(a.cw));
+    float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
+    for (int i = threadIdx.x; i < a.ntab; i += blockDim.x) tab[i] = a.row_tab[i];
+    if (threadIdx.x == 0) sh.next_task = 0;
+    __syncthreads();
+    const long nitems = p1_items(a, 32 * KU);
+    for (long it = blockIdx.x; it < nitems; it += gridDim.x)
+        p1_item<IDX, TAB_HALF, BIG, KU>(a, it, stage, info_all, tab, sh);
+}
+
+// Batched pass 1: the work items of many matrices (item_begin: first item of
+// each matrix, item_begin[nmat] = total) handed out by a device work queue,
+// one item per grab.  Items are grabbed in increasing order, so a CTA moves
+// forward through the matrices and reloads the twiddle table only when it
+// enters a new one.  *queue must be 0 at launch.
+template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+__global__ void __launch_bounds__(P1_THREADS, 1)
+k_twiddle_sum_batch(const P1Args* __restrict__ args, const long* __restrict__ item_begin, int nmat,
+                    unsigned long long* queue) {
+    extern __shared__ float4 smem_raw[];
+    __shared__ P1Shared sh;
+    __shared__ P1Args cur;
+    __shared__ long s_it;
+    __shared__ int s_m;
+    float2* stage = reinterpret_cast<float2*>(smem_raw);
+    int loaded = -1;
+    if (threadIdx.x == 0) { sh.next_task = 0; s_m = 0; }
+    __syncthreads();
+    const long total = item_begin[nmat];
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long it = (long)atomicAdd(queue, 1ull);
+            int m = s_m;
+            while (m < nmat && item_begin[m + 1] <= it) m++;
+            s_it = it;
+            s_m = m;
+        }
         __syncthreads();
+        const long it = s_it;
+        const int m = s_m;
+        if (it >= total) break;
+        if (m != loaded) {
+            if (threadIdx.x == 0) cur = args[m];
+            __syncthreads();
+            NzInfo* info_all = reinterpret_cast<NzInfo*>(stage + (size_t)32 * KU * p1_pitch(cur.cw));
+            float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
+            for (int i = threadIdx.x; i < cur.ntab; i += blockDim.x) tab[i] = cur.row_tab[i];
+            __syncthreads();
+            loaded = m;
+        }
+        NzInfo* info_all = reinterpret_cast<NzInfo*>(stage + (size_t)32 * KU * p1_pitch(cur.cw));
+        float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
+        p1_item<IDX, TAB_HALF, BIG, KU>(cur, it - item_begin[m], stage, info_all, tab, sh);
     }
 }
 
@@ -459,26 +528,129 @@ k_twiddle_sum(const IDX* __restrict__ row_idx, const uint8_t* __restrict__ win_s
 // per stage (src/sparse_fft_bluestein.cu:2327-2370) and writes 8-byte stores
 // in bluestein_finalize_kernel (:469-486).
 // ---------------------------------------------------------------------------
+// One matrix's row-kernel inputs for one tile of Bluestein rows [u0, u0+tile_rows).
+struct RowsArgs {
+    const float2* S;
+    size_t s_pitch;
+    const float2* pre;
+    const float2* post;
+    const float2* filt;
+    const float2* fft_tw;
+    float2* out;
+    size_t out_pitch;
+    int K, rows, cols, u0, tile_rows;
+};
+
+// One Bluestein row t of the tile (u = u0 + t), channel q of K: input,
+// forward network, filter, inverse network, Hermitian-paired output.  Whole
+// CTA (with the cluster when K > 1); ends on a barrier, so the next row may
+// overwrite buf at once.
+template <int MAXR>
+__device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& fd, int t, int q, float2* buf,
+                                              const float2* twr, const float2* const* zsrc, uint64_t* bar,
+                                              uint32_t& parity, bool& timed_out) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int Lp = fd.Lp, K = a.K, cols = a.cols;
+    const bool CLUSTER = K > 1;
+    const float2* preq = a.pre + (size_t)q * cols;
+    const float2* filtq = a.filt + (size_t)q * Lp;
+    const int half_slots = (int)(a.out_pitch >> 1);
+    const int hc = cols / 2;
+    const int cols_even = (cols + 1) & ~1;
+    // stage 0 twiddles stream from global memory, the rest sit in shared memory
+    auto tw_of = [&](int s) -> const float2* {
+        return (s == 0) ? a.fft_tw + fd.twoff[0] : twr + (fd.twoff[s] - fd.rest_base);
+    };
+    const int u = a.u0 + t;
+    const float2* srow = a.S + (size_t)t * a.s_pitch;
+    if (cols_even <= Lp) {
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            mbar_expect_tx(bar, (uint32_t)cols_even * 8u);
+            bulk_copy_g2s(buf, srow, (uint32_t)cols_even * 8u, bar);
+        }
+        for (int i = cols_even + tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
+        if (!mbar_wait_bounded(bar, parity)) timed_out = true;
+        parity ^= 1u;
+        if (q != 0)  // channel pre-twiddle (channel 0's is 1)
+            for (int c = tid; c < cols; c += nt) buf[c] = cmul(buf[c], __ldg(preq + c));
+        __syncthreads();
+    } else {
+        for (int i = tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
+        __syncthreads();
+        // several input columns fold onto one slot: add section by section
+        for (int lo = 0; lo < cols; lo += Lp) {
+            const int hi = min(cols, lo + Lp);
+            for (int c = lo + tid; c < hi; c += nt)
+                buf[c - lo] = cadd(buf[c - lo], cmul(__ldcs(srow + c), __ldg(preq + c)));
+            __syncthreads();
+        }
+    }
+    // forward DIF, filter multiply fused with the last stage, inverse DIT
+    const int S1 = fd.nst - 1;
+    for (int s = 0; s < S1; s++) {
+        fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s), (const float2*)nullptr,
+                                    tid, nt);
+        __syncthreads();
+    }
+    fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
+    __syncthreads();
+    for (int s = S1 - 1; s >= 0; s--) {
+        fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s), (const float2*)nullptr,
+                                    tid, nt);
+        __syncthreads();
+    }
+    if (CLUSTER) cg::this_cluster().sync();
+
+    // Hermitian-paired row writer
+    const int u2 = (u == 0) ? 0 : a.rows - u;
+    const bool two = (u2 != u);
+    const int nslots = two ? 2 * half_slots : half_slots;
+    const int lo = (int)((long)q * nslots / K), hi = (int)((long)(q + 1) * nslots / K);
+    for (int s = lo + tid; s < hi; s += nt) {
+        const int sel = s >= half_slots;
+        const int v = 2 * (s - sel * half_slots);
+        float2 o[2];
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            const int vv = v + e;
+            float2 val = make_float2(0.f, 0.f);
+            if (vv <= hc) {
+                const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
+                if (CLUSTER) {
+                    int n = c;
+                    while (n >= Lp) n -= Lp;
+                    for (int qq = 0; qq < K; qq++)
+                        val = cadd(val, cmul(zsrc[qq][n], __ldg(a.post + (size_t)qq * cols + c)));
+                } else {
+                    val = cmul(buf[c], __ldg(a.post + c));
+                }
+                if (sel) val.y = -val.y;
+            }
+            o[e] = val;
+        }
+        const int row = sel ? u2 : u;
+        float4* dst = reinterpret_cast<float4*>(a.out + (size_t)row * a.out_pitch + v);
+        __stcs(dst, make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
+    }
+    if (CLUSTER) cg::this_cluster().sync();
+    else __syncthreads();
+}
+
 template <int NTMAX>
-__global__ void __launch_bounds__(NTMAX, 1)
-k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, const float2* __restrict__ pre,
-                 const float2* __restrict__ post, const float2* __restrict__ filt,
-                 const float2* __restrict__ fft_tw, FFTDesc fd, int K, int rows, int cols,
-                 int u0, int tile_rows, float2* __restrict__ out, size_t out_pitch, int* err) {
+__global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc fd, int* err) {
     extern __shared__ float4 smem_raw[];
     __shared__ uint64_t in_bar;
     float2* buf = reinterpret_cast<float2*>(smem_raw);
-    const int Lp = fd.Lp;
-    float2* twr = buf + Lp;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int i = tid; i < fd.rest_len; i += nt) twr[i] = fft_tw[fd.rest_base + i];
-    if (tid == 0) mbar_init(&in_bar, 1);
+    float2* twr = buf + fd.Lp;
+    for (int i = threadIdx.x; i < fd.rest_len; i += blockDim.x) twr[i] = a.fft_tw[fd.rest_base + i];
+    if (threadIdx.x == 0) mbar_init(&in_bar, 1);
 
     constexpr int MAXR = (NTMAX > 512) ? MAX_RADIX_NT1024 : MAX_RADIX_NT512;
-    const bool CLUSTER = K > 1;  // K > 1 only in launches with a K-CTA cluster dimension
+    const int K = a.K;  // K > 1 only in launches with a K-CTA cluster dimension
     int q = 0, cid = blockIdx.x, ncl = gridDim.x;
     const float2* zsrc[MAX_CHANNELS];
-    if (CLUSTER) {
+    if (K > 1) {
         cg::cluster_group cl = cg::this_cluster();
         q = (int)cl.block_rank();
         cid = blockIdx.x / K;
@@ -489,100 +661,79 @@ k_bluestein_rows(const float2* __restrict__ S, size_t s_pitch, const float2* __r
     } else {
         zsrc[0] = buf;
     }
-    const float2* preq = pre + (size_t)q * cols;
-    const float2* filtq = filt + (size_t)q * Lp;
-    const int half_slots = (int)(out_pitch >> 1);
-    const int hc = cols / 2;
-    const int cols_even = (cols + 1) & ~1;
-    const bool bulk_in = cols_even <= Lp;
-    // stage 0 twiddles stream from global memory, the rest sit in shared memory
-    auto tw_of = [&](int s) -> const float2* {
-        return (s == 0) ? fft_tw + fd.twoff[0] : twr + (fd.twoff[s] - fd.rest_base);
-    };
     uint32_t parity = 0;
     bool timed_out = false;
     __syncthreads();
-
-    for (int t = cid; t < tile_rows; t += ncl) {
-        const int u = u0 + t;
-        const float2* srow = S + (size_t)t * s_pitch;
-        if (bulk_in) {
-            if (tid == 0) {
-                fence_proxy_async_smem();
-                mbar_expect_tx(&in_bar, (uint32_t)cols_even * 8u);
-                bulk_copy_g2s(buf, srow, (uint32_t)cols_even * 8u, &in_bar);
-            }
-            for (int i = cols_even + tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
-            if (!mbar_wait_bounded(&in_bar, parity)) timed_out = true;
-            parity ^= 1u;
-            if (q != 0)  // channel pre-twiddle (channel 0's is 1)
-                for (int c = tid; c < cols; c += nt) buf[c] = cmul(buf[c], __ldg(preq + c));
-            __syncthreads();
-        } else {
-            for (int i = tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
-            __syncthreads();
-            // several input columns fold onto one slot: add section by section
-            for (int lo = 0; lo < cols; lo += Lp) {
-                const int hi = min(cols, lo + Lp);
-                for (int c = lo + tid; c < hi; c += nt)
-                    buf[c - lo] = cadd(buf[c - lo], cmul(__ldcs(srow + c), __ldg(preq + c)));
-                __syncthreads();
-            }
-        }
-        // forward DIF, filter multiply fused with the last stage, inverse DIT
-        const int S1 = fd.nst - 1;
-        for (int s = 0; s < S1; s++) {
-            fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                        (const float2*)nullptr, tid, nt);
-            __syncthreads();
-        }
-        fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
-        __syncthreads();
-        for (int s = S1 - 1; s >= 0; s--) {
-            fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                        (const float2*)nullptr, tid, nt);
-            __syncthreads();
-        }
-        if (CLUSTER) cg::this_cluster().sync();
-
-        // Hermitian-paired row writer
-        const int u2 = (u == 0) ? 0 : rows - u;
-        const bool two = (u2 != u);
-        const int nslots = two ? 2 * half_slots : half_slots;
-        const int lo = (int)((long)q * nslots / K), hi = (int)((long)(q + 1) * nslots / K);
-        for (int s = lo + tid; s < hi; s += nt) {
-            const int sel = s >= half_slots;
-            const int v = 2 * (s - sel * half_slots);
-            float2 o[2];
-#pragma unroll
-            for (int e = 0; e < 2; e++) {
-                const int vv = v + e;
-                float2 val = make_float2(0.f, 0.f);
-                if (vv <= hc) {
-                    const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
-                    if (CLUSTER) {
-                        int n = c;
-                        while (n >= Lp) n -= Lp;
-                        for (int qq = 0; qq < K; qq++)
-                            val = cadd(val, cmul(zsrc[qq][n], __ldg(post + (size_t)qq * cols + c)));
-                    } else {
-                        val = cmul(buf[c], __ldg(post + c));
-                    }
-                    if (sel) val.y = -val.y;
-                }
-                o[e] = val;
-            }
-            const int row = sel ? u2 : u;
-            float4* dst = reinterpret_cast<float4*>(out + (size_t)row * out_pitch + v);
-            __stcs(dst, make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
-        }
-        if (CLUSTER) cg::this_cluster().sync();
-        else __syncthreads();
-    }
+    for (int t = cid; t < a.tile_rows; t += ncl)
+        bluestein_row<MAXR>(a, fd, t, q, buf, twr, zsrc, &in_bar, parity, timed_out);
     if (timed_out) {
         atomicOr(err, ERR_TIMEOUT);
         // a copy that never signalled may still be in flight: wait once more
         // (bounded) before the shared memory is released
+        mbar_wait_bounded(&in_bar, parity ^ 1u);
+    }
+}
+
+// Batched rows: the Bluestein rows of many single-channel matrices
+// (row_begin: first row of each matrix in the queue, row_begin[nmat] =
+// total) handed out one at a time by a device work queue.  A CTA enters the
+// matrices in order and reloads the matrix's descriptor and stage twiddles
+// only when it moves to the next one.  Shared memory holds the largest
+// matrix's row buffer plus its stage twiddles (the twiddles of each matrix
+// sit right after its own row buffer).  *queue must be 0 at launch.
+struct RowsBatch {
+    RowsArgs a;
+    FFTDesc fd;
+};
+
+template <int NTMAX>
+__global__ void __launch_bounds__(NTMAX, 1)
+k_bluestein_rows_batch(const RowsBatch* __restrict__ descs, const long* __restrict__ row_begin, int nmat,
+                       unsigned long long* queue, int* err) {
+    extern __shared__ float4 smem_raw[];
+    __shared__ uint64_t in_bar;
+    __shared__ RowsBatch cur;
+    __shared__ long s_t;
+    __shared__ int s_m;
+    constexpr int MAXR = (NTMAX > 512) ? MAX_RADIX_NT1024 : MAX_RADIX_NT512;
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    float2* twr = buf;
+    if (threadIdx.x == 0) {
+        mbar_init(&in_bar, 1);
+        s_m = 0;
+    }
+    const float2* zsrc[1] = {buf};
+    uint32_t parity = 0;
+    bool timed_out = false;
+    int loaded = -1;
+    const long total = row_begin[nmat];
+    __syncthreads();
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long t = (long)atomicAdd(queue, 1ull);
+            int m = s_m;
+            while (m < nmat && row_begin[m + 1] <= t) m++;
+            s_t = t;
+            s_m = m;
+        }
+        __syncthreads();
+        const long t = s_t;
+        const int m = s_m;
+        if (t >= total) break;
+        if (m != loaded) {
+            if (threadIdx.x == 0) cur = descs[m];
+            __syncthreads();
+            twr = buf + cur.fd.Lp;
+            for (int i = threadIdx.x; i < cur.fd.rest_len; i += blockDim.x)
+                twr[i] = cur.a.fft_tw[cur.fd.rest_base + i];
+            __syncthreads();
+            loaded = m;
+        }
+        bluestein_row<MAXR>(cur.a, cur.fd, (int)(t - row_begin[m]), 0, buf, twr, zsrc, &in_bar, parity,
+                            timed_out);
+    }
+    if (timed_out) {
+        atomicOr(err, ERR_TIMEOUT);
         mbar_wait_bounded(&in_bar, parity ^ 1u);
     }
 }

@@ -75,6 +75,20 @@ int dev_alloc(gbsp_plan_s* p, void** ptr, size_t bytes) {
     return GBSP_OK;
 }
 
+// Lets `kern` take all the opt-in shared memory of a CTA.  The limit is a
+// property of the kernel, shared by every plan in the process; one fixed
+// value keeps a later, smaller plan from invalidating an earlier one.
+template <typename F>
+int allow_full_smem(F* kern) {
+    cudaFuncAttributes fa;
+    int dev = 0, optin = 0;
+    GB_CUDA(cudaFuncGetAttributes(&fa, kern));
+    GB_CUDA(cudaGetDevice(&dev));
+    GB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    return GBSP_OK;
+}
+
 void free_plan(gbsp_plan_s* p) {
     if (!p) return;
     for (void* a : p->allocs) cudaFree(a);
@@ -123,11 +137,15 @@ size_t rows_smem_bytes(const gbsp::FFTDesc& fd) {
 // Every multiset of supported radices whose product is the channel length
 // (at most 7 stages) is ordered even radices first, odd radices last (an odd
 // radix at span 1 keeps the last stage free of bank conflicts) and scored by
-// a model of one row's work on a block of nt threads: thread slots actually
-// occupied (ceil(butterflies / nt) rounds of nt threads x radix), a cost per
-// barrier, a penalty for strided shared-memory patterns, and a small one for
-// few resident warps.  The exhaustive tuner can override the choice.
-const int kRadices[] = {49, 40, 35, 32, 28, 25, 24, 21, 20, 16, 15, 14, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+// a model fitted to GB300 measurements of the row kernel: a stage costs
+// (rounds of the block over its butterflies) x radix, forward and inverse
+// stages twice, the fused middle stage 1.6 times, radices above 32 a little
+// more (register pressure), plus a fixed cost per stage; the row time is that
+// cost divided by the CTAs resident per SM (a 512-thread block at 128
+// registers fills an SM's register file, smaller blocks can pair up when
+// shared memory allows).  Block sizes 256 and 512 are considered; 1024 only
+// on request.  The tuner can override the choice by measurement.
+const int kRadices[] = {40, 35, 32, 28, 25, 24, 21, 20, 16, 15, 12, 9, 8, 7, 5, 4, 3, 2};
 
 void factorizations(int rem, int maxr, std::vector<int>& cur, std::vector<std::vector<int>>& out) {
     if (rem == 1) {
@@ -155,19 +173,25 @@ std::vector<int> order_radices(std::vector<int> rs) {
 // largest radix a block of the given maximum size can hold in registers
 inline int max_radix_for(int nt_max) { return nt_max > 512 ? gbsp::MAX_RADIX_NT1024 : gbsp::MAX_RADIX_NT512; }
 
-double rows_cost(const gbsp::FFTDesc& fd, int nt) {
+// SM limits the model uses (GB300: 228 KB shared memory, 64K registers, 2048 threads per SM)
+constexpr size_t kSmemPerSM = 233472;
+constexpr int kRegsPerSM = 65536;
+
+double rows_cost(const gbsp::FFTDesc& fd, int nt, size_t smem_per_cta) {
     double cost = 0.0;
     for (int s = 0; s < fd.nst; s++) {
         const int R = fd.R[s], m = fd.m[s], nb = fd.Lp / R, l = nb / m;
         const double rounds = std::ceil((double)nb / (double)nt);
-        double per = rounds * nt * R * (1.0 + 0.08 * std::log2((double)R));
+        double per = rounds * R * (R > 32 ? 1.1 : 1.0);
         const bool strided = (m == 1 && R % 2 == 0) ||
                              (m > 1 && m < 16 && l > 1 && !gbsp::stage_j_fastest(R, m, l));
         if (strided) per *= 1.5;
-        per += 0.25 * fd.Lp;
-        cost += (s == fd.nst - 1) ? 1.6 * per : 2.0 * per;
+        cost += ((s == fd.nst - 1) ? 1.6 : 2.0) * per + 12.0;
     }
-    return cost * (1.0 + 0.15 * 512.0 / nt);
+    const int regs = nt <= 512 ? 128 : 64;
+    int ctas = std::min({(int)(kSmemPerSM / (smem_per_cta + 1024)), 2048 / nt, kRegsPerSM / (nt * regs)});
+    ctas = std::max(ctas, 1);
+    return cost / ctas;
 }
 
 struct RadixPlan {
@@ -197,9 +221,9 @@ bool plan_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt, Rad
         const int rmax = *std::max_element(rs.begin(), rs.end());
         const int nt_hi = rmax > max_radix_for(1024) ? 512 : 1024;
         if (rmax > max_radix_for(512)) continue;
-        for (int nt = 64; nt <= nt_hi; nt += 32) {
-            if (nt_opt > 0 && nt != nt_opt) continue;
-            const double c = rows_cost(fd, nt);
+        for (int nt : {256, 512, 1024, nt_opt}) {
+            if (nt <= 0 || nt > nt_hi || (nt_opt > 0 && nt != nt_opt) || (nt_opt == 0 && nt == 1024)) continue;
+            const double c = rows_cost(fd, nt, rows_smem_bytes(fd));
             if (c < best->cost) {
                 best->cost = c;
                 best->fd = fd;
@@ -214,7 +238,7 @@ bool plan_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt, Rad
 template <typename IDX, bool HALF, bool BIG, int KU>
 int p1_prepare(gbsp_plan_s* p, int sms) {
     auto kern = gbsp::k_twiddle_sum<IDX, HALF, BIG, KU>;
-    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->p1_smem));
+    if (int rc = allow_full_smem(kern)) return rc;
     int nb = 0;
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, gbsp::P1_THREADS, p->p1_smem));
     if (nb < 1) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 kernel does not fit on an SM");
@@ -222,12 +246,33 @@ int p1_prepare(gbsp_plan_s* p, int sms) {
     return GBSP_OK;
 }
 
+gbsp::P1Args p1_args(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pitch, const float2* chirp) {
+    gbsp::P1Args a;
+    a.row_idx = p->d_row_idx;
+    a.win_slot0 = p->d_win_slot0;
+    a.win_task = p->d_win_task;
+    a.win_task_col = p->d_win_task_col;
+    a.row_tab = p->d_rowtab;
+    a.chirp = chirp;
+    a.S = S;
+    a.s_pitch = s_pitch;
+    a.cw = p->p1_cw;
+    a.cols = p->cols;
+    a.s_cols = p->s_cols;
+    a.ntab = p->ntab;
+    a.rows = p->rows;
+    a.u0 = u0;
+    a.tile_rows = n;
+    a.kahan_min = p->kahan_min;
+    a.magic = p->rows_magic;
+    return a;
+}
+
 template <typename IDX, bool HALF, bool BIG, int KU>
 void p1_launch(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pitch, const float2* chirp,
                cudaStream_t st) {
     gbsp::k_twiddle_sum<IDX, HALF, BIG, KU><<<p->p1_grid, gbsp::P1_THREADS, p->p1_smem, st>>>(
-        (const IDX*)p->d_row_idx, p->d_win_slot0, p->d_win_task, p->d_win_task_col, p->p1_cw, p->cols,
-        p->s_cols, p->d_rowtab, p->ntab, p->rows, p->rows_magic, chirp, u0, n, S, s_pitch, p->kahan_min);
+        p1_args(p, u0, n, S, s_pitch, chirp));
 }
 
 // prepare == true: set attributes and grid; false: launch
@@ -295,7 +340,7 @@ cudaLaunchConfig_t rows_config(const gbsp_plan_s* p, unsigned grid, unsigned nt,
 template <bool CL, int NTMAX>
 int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
     auto kern = gbsp::k_bluestein_rows<NTMAX>;
-    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->rows_smem));
+    if (int rc = allow_full_smem(kern)) return rc;
     *cap = 0;
     if (!CL) {
         int nb = 0;
@@ -309,14 +354,31 @@ int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
     return GBSP_OK;
 }
 
+gbsp::RowsArgs rows_args(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
+                         size_t out_pitch) {
+    gbsp::RowsArgs a;
+    a.S = S;
+    a.s_pitch = s_pitch;
+    a.pre = p->d_pre;
+    a.post = p->d_post;
+    a.filt = p->d_filt;
+    a.fft_tw = p->d_fftw;
+    a.out = (float2*)d_out;
+    a.out_pitch = out_pitch;
+    a.K = p->K;
+    a.rows = p->rows;
+    a.cols = p->cols;
+    a.u0 = u0;
+    a.tile_rows = n;
+    return a;
+}
+
 template <bool CL, int NTMAX>
 int rows_launch_t(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch, cudaStream_t st) {
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>, (const float2*)p->d_S,
-                               p->s_pitch, (const float2*)p->d_pre, (const float2*)p->d_post,
-                               (const float2*)p->d_filt, (const float2*)p->d_fftw, p->fd, p->K,
-                               p->rows, p->cols, u0, n, (float2*)d_out, out_pitch, p->d_err));
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>,
+                               rows_args(p, p->d_S, p->s_pitch, u0, n, d_out, out_pitch), p->fd, p->d_err));
     return GBSP_OK;
 }
 
@@ -370,8 +432,10 @@ int validate_csc(int rows, int cols, int n_active, int nnz, const int* col_ptr,
     return GBSP_OK;
 }
 
+// force_p1: {ku, cw, half} imposes the pass-1 shape (batches need one shape
+// for all their matrices); nullptr chooses it from the shared-memory budget.
 int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int* sparse_cols,
-               const gbsp_options* o, cudaStream_t st) {
+               const gbsp_options* o, cudaStream_t st, const int* force_p1 = nullptr) {
     const int policy = (o && o->length_policy) ? o->length_policy : GBSP_LEN_3SMOOTH;
     if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH)
         return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: length_policy must be 3 or 7");
@@ -429,6 +493,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         bool ok = false;
         for (const Shape& sh : shapes) {
             if ((tmode == 1 && sh.half) || (tmode == 2 && !sh.half)) continue;
+            if (force_p1 && (sh.ku != force_p1[0] || sh.cw != force_p1[1] || sh.half != force_p1[2])) continue;
             const size_t ntab = sh.half ? (size_t)(p->rows / 2 + 1) : (size_t)p->rows;
             const size_t bytes = gbsp::p1_head_bytes(sh.ku, sh.cw) + ntab * sizeof(float2);
             if (bytes + 1024 > smem_cap) continue;  // static shared variables
@@ -738,9 +803,8 @@ int rows_launch_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int 
                      size_t out_pitch, cudaStream_t st) {
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>, S, s_pitch, (const float2*)p->d_pre,
-                               (const float2*)p->d_post, (const float2*)p->d_filt, (const float2*)p->d_fftw,
-                               p->fd, p->K, p->rows, p->cols, u0, n, (float2*)d_out, out_pitch, p->d_err));
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>,
+                               rows_args(p, S, s_pitch, u0, n, d_out, out_pitch), p->fd, p->d_err));
     return GBSP_OK;
 }
 
@@ -782,3 +846,337 @@ extern "C" int gbsp_execute_noalloc(gbsp_plan_t p, void* d_out, size_t out_pitch
     }
     return GBSP_OK;
 }
+
+// ===========================================================================
+// Batches: many matrices of uneven size and sparsity in one persistent
+// launch per pass, fed by device work queues.
+//
+// Each matrix gets its own tables and scratch (a plan built with a pass-1
+// shape and a block size common to the batch); one descriptor per matrix
+// lists them.  gbsp_batch_execute resets the two queue heads and launches
+// k_twiddle_sum_batch and k_bluestein_rows_batch once each; matrices whose
+// convolution needs several channels run after them through their own plan.
+// The three operations capture into a CUDA graph (gbsp_batch_graph_*).
+// ===========================================================================
+struct gbsp_batch_s {
+    int count = 0;
+    int device = 0;
+    std::vector<gbsp_plan_s*> plans;
+    std::vector<int> order;      // queue order (batched matrices, costliest rows first)
+    std::vector<int> separate;   // matrices that run through their own plan
+    int ku = 8, cw = 32, half = 0, idx_bytes = 2, big = 0;
+    int p1_grid = 0;
+    size_t p1_smem = 0;
+    int rows_grid = 0, rows_threads = 512;
+    size_t rows_smem = 0;
+    gbsp::P1Args* d_p1 = nullptr;
+    long* d_p1_begin = nullptr;
+    gbsp::RowsBatch* d_rows = nullptr;
+    long* d_row_begin = nullptr;
+    unsigned long long* d_queue = nullptr;  // [0] pass 1, [1] rows
+    int* d_err = nullptr;
+    std::vector<void*> outs;
+    std::vector<size_t> pitches;
+    bool outputs_set = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+void free_batch(gbsp_batch_s* b) {
+    if (!b) return;
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto* p : b->plans) free_plan(p);
+    for (void* a : b->allocs) cudaFree(a);
+    delete b;
+}
+
+int batch_alloc(gbsp_batch_s* b, void** ptr, size_t bytes) {
+    cudaError_t e = cudaMalloc(ptr, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(GBSP_ERR_ALLOC, std::string("batch cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    b->allocs.push_back(*ptr);
+    return GBSP_OK;
+}
+
+template <typename IDX, bool HALF, bool BIG, int KU>
+int p1b_run(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
+    auto kern = gbsp::k_twiddle_sum_batch<IDX, HALF, BIG, KU>;
+    if (prepare) {
+        if (int rc = allow_full_smem(kern)) return rc;
+        int nb = 0;
+        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, gbsp::P1_THREADS, b->p1_smem));
+        if (nb < 1) return set_error(GBSP_ERR_UNSUPPORTED, "batched pass 1 does not fit on an SM");
+        b->p1_grid = nb * sms;
+        return GBSP_OK;
+    }
+    kern<<<b->p1_grid, gbsp::P1_THREADS, b->p1_smem, st>>>(b->d_p1, b->d_p1_begin, (int)b->order.size(),
+                                                            b->d_queue);
+    GB_CUDA(cudaGetLastError());
+    return GBSP_OK;
+}
+
+template <typename IDX, bool HALF, bool BIG>
+int p1b_ku(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
+    return b->ku == 8 ? p1b_run<IDX, HALF, BIG, 8>(b, prepare, sms, st) : p1b_run<IDX, HALF, BIG, 4>(b, prepare, sms, st);
+}
+
+template <bool HALF>
+int p1b_half(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
+    if (b->idx_bytes == 2) return p1b_ku<uint16_t, HALF, false>(b, prepare, sms, st);
+    if (b->big) return p1b_ku<uint32_t, HALF, true>(b, prepare, sms, st);
+    return p1b_ku<uint32_t, HALF, false>(b, prepare, sms, st);
+}
+
+int p1b_dispatch(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
+    return b->half ? p1b_half<true>(b, prepare, sms, st) : p1b_half<false>(b, prepare, sms, st);
+}
+
+int batch_launch(gbsp_batch_s* b, cudaStream_t st) {
+    if (!b->order.empty()) {
+        GB_CUDA(cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(unsigned long long), st));
+        int rc = p1b_dispatch(b, false, 0, st);
+        if (rc) return rc;
+        gbsp::k_bluestein_rows_batch<512><<<b->rows_grid, b->rows_threads, b->rows_smem, st>>>(
+            b->d_rows, b->d_row_begin, (int)b->order.size(), b->d_queue + 1, b->d_err);
+        GB_CUDA(cudaGetLastError());
+    }
+    for (int m : b->separate) {
+        int rc = gbsp_execute(b->plans[m], b->outs[m], b->pitches[m], st);
+        if (rc) return rc;
+    }
+    return GBSP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* opts, void* stream,
+                      gbsp_batch_t* out) {
+    if (!out || count < 1 || !mats) return set_error(GBSP_ERR_INVALID, "gbsp_batch_create: bad arguments");
+    *out = nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    gbsp_batch_s* b = new (std::nothrow) gbsp_batch_s();
+    if (!b) return set_error(GBSP_ERR_ALLOC, "gbsp_batch_create: out of host memory");
+    b->count = count;
+    int rc = GBSP_OK;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&b->device) != cudaSuccess || cudaGetDeviceProperties(&prop, b->device) != cudaSuccess) {
+        free_batch(b);
+        return set_error(GBSP_ERR_CUDA, "gbsp_batch_create: no CUDA device");
+    }
+    const size_t smem_cap = prop.sharedMemPerBlockOptin;
+    const int sms = prop.multiProcessorCount;
+    // one pass-1 shape for the batch: the largest row count decides it
+    int max_rows = 1;
+    bool u32 = false;
+    for (int i = 0; i < count; i++) {
+        int vr = validate_csc(mats[i].rows, mats[i].cols, mats[i].n_active, mats[i].nnz, mats[i].col_ptr,
+                              mats[i].row_idx, mats[i].sparse_cols);
+        if (vr) {
+            free_batch(b);
+            return vr;
+        }
+        max_rows = std::max(max_rows, mats[i].rows);
+        u32 = u32 || mats[i].rows > 65536 || mats[i].cols > 65536 || (opts && opts->index_bytes == 4);
+    }
+    b->idx_bytes = u32 ? 4 : 2;
+    b->big = max_rows > 65535;
+    {
+        struct Shape { int ku, cw, half; };
+        const Shape shapes[] = {{8, 32, 0}, {8, 32, 1}, {4, 64, 0}, {4, 32, 0}, {4, 64, 1}, {4, 32, 1}};
+        bool ok = false;
+        const int tmode = opts ? opts->row_table_mode : 0;
+        for (const Shape& sh : shapes) {
+            if ((tmode == 1 && sh.half) || (tmode == 2 && !sh.half)) continue;
+            const size_t ntab = sh.half ? (size_t)(max_rows / 2 + 1) : (size_t)max_rows;
+            const size_t bytes = gbsp::p1_head_bytes(sh.ku, sh.cw) + ntab * sizeof(float2);
+            if (bytes + 1024 > smem_cap) continue;
+            b->ku = sh.ku;
+            b->cw = sh.cw;
+            b->half = sh.half;
+            b->p1_smem = bytes;
+            ok = true;
+            break;
+        }
+        if (!ok) {
+            free_batch(b);
+            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: rows too large for the pass-1 table");
+        }
+    }
+    // one plan per matrix with the common shape and a 512-thread row block
+    gbsp_options o = opts ? *opts : gbsp_options{};
+    o.u_tile = 0;
+    o.index_bytes = b->idx_bytes;
+    o.rows_threads = b->rows_threads;
+    o.row_table_mode = b->half ? 2 : 1;
+    for (int& r : o.radix) r = 0;  // lengths differ across the batch: auto radices
+    const int force[3] = {b->ku, b->cw, b->half};
+    b->plans.assign(count, nullptr);
+    for (int i = 0; i < count && rc == GBSP_OK; i++) {
+        gbsp_plan_s* p = new (std::nothrow) gbsp_plan_s();
+        if (!p) { rc = set_error(GBSP_ERR_ALLOC, "gbsp_batch_create: out of host memory"); break; }
+        p->rows = mats[i].rows;
+        p->cols = mats[i].cols;
+        p->nnz = mats[i].nnz;
+        p->n_active = mats[i].n_active;
+        b->plans[i] = p;
+        rc = plan_build(p, mats[i].col_ptr, mats[i].row_idx, mats[i].sparse_cols, &o, st, force);
+    }
+    if (rc) {
+        free_batch(b);
+        return rc;
+    }
+    // queue order: single-channel matrices by decreasing channel length
+    for (int i = 0; i < count; i++) (b->plans[i]->K == 1 ? b->order : b->separate).push_back(i);
+    std::stable_sort(b->order.begin(), b->order.end(),
+                     [&](int x, int y) { return b->plans[x]->Lp > b->plans[y]->Lp; });
+    b->rows_smem = 0;
+    for (int m : b->order) {
+        b->rows_smem = std::max(b->rows_smem, rows_smem_bytes(b->plans[m]->fd));
+    }
+    const int n = (int)b->order.size();
+    if (n > 0) {
+        if (b->rows_smem + 1024 > smem_cap) {
+            free_batch(b);
+            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: batch row buffer exceeds shared memory");
+        }
+        if ((rc = p1b_dispatch(b, true, sms, st)) ||
+            (rc = batch_alloc(b, (void**)&b->d_p1, sizeof(gbsp::P1Args) * n)) ||
+            (rc = batch_alloc(b, (void**)&b->d_p1_begin, sizeof(long) * (n + 1))) ||
+            (rc = batch_alloc(b, (void**)&b->d_rows, sizeof(gbsp::RowsBatch) * n)) ||
+            (rc = batch_alloc(b, (void**)&b->d_row_begin, sizeof(long) * (n + 1)))) {
+            free_batch(b);
+            return rc;
+        }
+        auto kern = gbsp::k_bluestein_rows_batch<512>;
+        int nb = 0;
+        if (allow_full_smem(kern) != GBSP_OK ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, b->rows_threads, b->rows_smem) != cudaSuccess ||
+            nb < 1) {
+            free_batch(b);
+            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: batched row kernel does not fit");
+        }
+        b->rows_grid = nb * sms;
+        // work-queue prefix sums
+        std::vector<gbsp::P1Args> p1(n);
+        std::vector<long> p1b(n + 1, 0), rb(n + 1, 0);
+        const int ublk = 32 * b->ku;
+        for (int k = 0; k < n; k++) {
+            const gbsp_plan_s* p = b->plans[b->order[k]];
+            p1[k] = p1_args(p, 0, p->half_rows, p->d_S, p->s_pitch, p->d_post);
+            p1b[k + 1] = p1b[k] + (long)((p->half_rows + ublk - 1) / ublk) * ((p->s_cols + p->p1_cw - 1) / p->p1_cw);
+            rb[k + 1] = rb[k] + p->half_rows;
+        }
+        if (cudaMemcpy(b->d_p1, p1.data(), sizeof(gbsp::P1Args) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->d_p1_begin, p1b.data(), sizeof(long) * (n + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->d_row_begin, rb.data(), sizeof(long) * (n + 1), cudaMemcpyHostToDevice) != cudaSuccess) {
+            free_batch(b);
+            return set_error(GBSP_ERR_CUDA, "gbsp_batch_create: descriptor upload failed");
+        }
+    }
+    if ((rc = batch_alloc(b, (void**)&b->d_queue, 2 * sizeof(unsigned long long))) ||
+        (rc = batch_alloc(b, (void**)&b->d_err, sizeof(int)))) {
+        free_batch(b);
+        return rc;
+    }
+    cudaMemset(b->d_err, 0, sizeof(int));
+    b->outs.assign(count, nullptr);
+    b->pitches.assign(count, 0);
+    *out = b;
+    return GBSP_OK;
+}
+
+int gbsp_batch_set_outputs(gbsp_batch_t b, void* const* d_outs, const size_t* out_pitches) {
+    if (!b || !d_outs || !out_pitches) return set_error(GBSP_ERR_INVALID, "gbsp_batch_set_outputs: null argument");
+    for (int i = 0; i < b->count; i++) {
+        int rc = check_out(b->plans[i], d_outs[i], out_pitches[i], "gbsp_batch_set_outputs");
+        if (rc) return rc;
+    }
+    const int n = (int)b->order.size();
+    std::vector<gbsp::RowsBatch> rows(n);
+    for (int k = 0; k < n; k++) {
+        const int m = b->order[k];
+        const gbsp_plan_s* p = b->plans[m];
+        rows[k].a = rows_args(p, p->d_S, p->s_pitch, 0, p->half_rows, d_outs[m], out_pitches[m]);
+        rows[k].fd = p->fd;
+    }
+    if (n > 0) GB_CUDA(cudaMemcpy(b->d_rows, rows.data(), sizeof(gbsp::RowsBatch) * n, cudaMemcpyHostToDevice));
+    for (int i = 0; i < b->count; i++) {
+        b->outs[i] = d_outs[i];
+        b->pitches[i] = out_pitches[i];
+    }
+    b->outputs_set = true;
+    if (b->graph_exec) {
+        cudaGraphExecDestroy(b->graph_exec);
+        b->graph_exec = nullptr;
+    }
+    return GBSP_OK;
+}
+
+int gbsp_batch_execute(gbsp_batch_t b, void* stream) {
+    if (!b) return set_error(GBSP_ERR_INVALID, "gbsp_batch_execute: null batch");
+    if (!b->outputs_set) return set_error(GBSP_ERR_INVALID, "gbsp_batch_execute: outputs not set");
+    return batch_launch(b, (cudaStream_t)stream);
+}
+
+int gbsp_batch_graph_launch(gbsp_batch_t b, void* stream) {
+    if (!b) return set_error(GBSP_ERR_INVALID, "gbsp_batch_graph_launch: null batch");
+    if (!b->outputs_set) return set_error(GBSP_ERR_INVALID, "gbsp_batch_graph_launch: outputs not set");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!b->graph_exec) {
+        // capture on a private stream so the caller's stream state is untouched
+        cudaStream_t cs = nullptr;
+        GB_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        int rc = (e == cudaSuccess) ? batch_launch(b, cs) : GBSP_ERR_CUDA;
+        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (e != cudaSuccess || e2 != cudaSuccess)
+            return set_error(GBSP_ERR_CUDA, "gbsp_batch_graph_launch: capture failed");
+        e = cudaGraphInstantiate(&b->graph_exec, g, 0);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->graph = g;
+        if (e != cudaSuccess) {
+            b->graph_exec = nullptr;
+            return set_error(GBSP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+    }
+    GB_CUDA(cudaGraphLaunch(b->graph_exec, st));
+    return GBSP_OK;
+}
+
+int gbsp_batch_error_flags(gbsp_batch_t b, int* flags) {
+    if (!b || !flags) return set_error(GBSP_ERR_INVALID, "gbsp_batch_error_flags: null argument");
+    int f = 0;
+    GB_CUDA(cudaMemcpy(&f, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
+    for (auto* p : b->plans) {
+        int g = 0;
+        GB_CUDA(cudaMemcpy(&g, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+        f |= g;
+    }
+    *flags = f;
+    return GBSP_OK;
+}
+
+int gbsp_batch_plan_info(gbsp_batch_t b, int i, gbsp_plan_info* info) {
+    if (!b || i < 0 || i >= b->count) return set_error(GBSP_ERR_INVALID, "gbsp_batch_plan_info: bad index");
+    return gbsp_plan_get_info(b->plans[i], info);
+}
+
+int gbsp_batch_destroy(gbsp_batch_t b) {
+    free_batch(b);
+    return GBSP_OK;
+}
+
+}  // extern "C"

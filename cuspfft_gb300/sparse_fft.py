@@ -14,7 +14,7 @@ from typing import Optional
 import numpy as np
 
 from . import _capi
-from ._capi import GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GbspOptions, GbspPlanInfo, check, load
+from ._capi import GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GbspMatrix, GbspOptions, GbspPlanInfo, check, load
 
 
 @dataclass
@@ -175,6 +175,95 @@ class Plan:
         if self._h:
             self._lib.gbsp_plan_destroy(self._h)
             self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Batch:
+    """Many matrices transformed together: one persistent launch per pass fed
+    by device work queues (gbsp_batch_* in include/gbspfft.h).
+
+    outputs are bound with set_outputs(); execute() enqueues the whole batch,
+    graph_launch() replays it as a CUDA graph.  Each output equals what
+    Plan(coo).execute() writes for the same matrix and options."""
+
+    def __init__(self, coos, *, length_policy: int = GBSP_LEN_3SMOOTH, kahan_min_degree: int = 0,
+                 index_bytes: int = 0, max_channel_len: int = 0, row_table_mode: int = 0, stream=None):
+        lib = load()
+        self._lib = lib
+        self._h = C.c_void_p()
+        self.shapes = [(c.rows, c.cols) for c in coos]
+        n = len(coos)
+        if n < 1:
+            raise ValueError("Batch needs at least one matrix")
+        keep = []
+        mats = (GbspMatrix * n)()
+        for i, coo in enumerate(coos):
+            csc = make_compact_csc(coo)
+            cp = np.ascontiguousarray(csc.col_ptr, np.int32)
+            ri = np.ascontiguousarray(csc.row_idx if coo.nnz else np.zeros(1, np.int32), np.int32)
+            sc = np.ascontiguousarray(csc.sparse_cols if csc.n_sparse_cols else np.zeros(1, np.int32), np.int32)
+            keep += [cp, ri, sc]
+            mats[i] = GbspMatrix(coo.rows, coo.cols, csc.n_sparse_cols, coo.nnz, _ip(cp), _ip(ri), _ip(sc))
+        o = GbspOptions(length_policy=length_policy, kahan_min_degree=kahan_min_degree, index_bytes=index_bytes,
+                        max_channel_len=max_channel_len, row_table_mode=row_table_mode)
+        check(lib.gbsp_batch_create(n, mats, C.byref(o), _stream_handle(stream), C.byref(self._h)),
+              "gbsp_batch_create")
+        self.infos = []
+        for i in range(n):
+            info = GbspPlanInfo()
+            check(lib.gbsp_batch_plan_info(self._h, i, C.byref(info)), "gbsp_batch_plan_info")
+            self.infos.append(info.as_dict())
+        self._outs = None
+
+    def __len__(self) -> int:
+        return len(self.shapes)
+
+    def empty_outputs(self):
+        import torch
+        return [torch.empty((r, info["output_pitch"]), dtype=torch.complex64, device="cuda")
+                for (r, _), info in zip(self.shapes, self.infos)]
+
+    def set_outputs(self, outs) -> None:
+        n = len(self.shapes)
+        if len(outs) != n:
+            raise ValueError(f"set_outputs needs {n} tensors")
+        for (r, _), out in zip(self.shapes, outs):
+            if str(out.dtype) != "torch.complex64" or not out.is_cuda or not out.is_contiguous():
+                raise ValueError("outputs must be contiguous complex64 CUDA tensors")
+            if out.dim() != 2 or out.shape[0] < r:
+                raise ValueError("each output must have shape (rows, pitch)")
+        ptrs = (C.c_void_p * n)(*[o.data_ptr() for o in outs])
+        pitches = (C.c_size_t * n)(*[o.shape[1] for o in outs])
+        check(self._lib.gbsp_batch_set_outputs(self._h, ptrs, pitches), "gbsp_batch_set_outputs")
+        self._outs = list(outs)  # keeps the memory alive while bound
+
+    def execute(self, stream=None) -> None:
+        check(self._lib.gbsp_batch_execute(self._h, _stream_handle(stream)), "gbsp_batch_execute")
+
+    def graph_launch(self, stream=None) -> None:
+        check(self._lib.gbsp_batch_graph_launch(self._h, _stream_handle(stream)), "gbsp_batch_graph_launch")
+
+    def error_flags(self) -> int:
+        f = C.c_int()
+        check(self._lib.gbsp_batch_error_flags(self._h, C.byref(f)), "gbsp_batch_error_flags")
+        return f.value
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.gbsp_batch_destroy(self._h)
+            self._h = C.c_void_p()
+        self._outs = None
 
     def __del__(self):
         try:

@@ -180,6 +180,42 @@ int gbsp_execute_noalloc(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* 
  * transform is not valid).  0 means no error was recorded. */
 int gbsp_plan_error_flags(gbsp_plan_t plan, int* flags);
 
+/* ---- batches ---------------------------------------------------------------
+ * Many matrices of uneven size and sparsity transformed by one persistent
+ * launch per pass, with work handed out by device queues: the GPU form of
+ * the reference's driver, which transforms one matrix per process
+ * (src/main.cu:249-311).  The reference has no batch entry point.
+ *
+ * gbsp_batch_create builds one sub-plan per matrix (same tables as
+ * gbsp_plan_create, with one pass-1 shape and a 512-thread row block common
+ * to the batch; explicit radices in opts are ignored).  Matrices whose
+ * convolution needs several channels (thread-block clusters) run after the
+ * batched launches through their own sub-plan.  Outputs are bound once with
+ * gbsp_batch_set_outputs (same rules as gbsp_execute's d_out / out_pitch);
+ * gbsp_batch_execute then enqueues the whole batch on `stream`.
+ * gbsp_batch_graph_launch does the same through a CUDA graph captured on
+ * its first call (and again after gbsp_batch_set_outputs).  Each output is
+ * identical to what gbsp_execute writes for the same matrix and options. */
+typedef struct gbsp_batch_s* gbsp_batch_t;
+
+typedef struct {
+    int rows, cols, n_active, nnz;
+    const int* col_ptr;      /* compact CSC as for gbsp_plan_create (host memory) */
+    const int* row_idx;
+    const int* sparse_cols;
+} gbsp_matrix;
+
+int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* opts, void* stream,
+                      gbsp_batch_t* batch);
+int gbsp_batch_set_outputs(gbsp_batch_t batch, void* const* d_outs, const size_t* out_pitches);
+int gbsp_batch_execute(gbsp_batch_t batch, void* stream);
+int gbsp_batch_graph_launch(gbsp_batch_t batch, void* stream);
+/* Plan details of matrix i (0-based, creation order). */
+int gbsp_batch_plan_info(gbsp_batch_t batch, int i, gbsp_plan_info* info);
+/* Reads and clears the device error flags of the batch and its sub-plans. */
+int gbsp_batch_error_flags(gbsp_batch_t batch, int* flags);
+int gbsp_batch_destroy(gbsp_batch_t batch);
+
 #ifdef __cplusplus
 }
 #endif
