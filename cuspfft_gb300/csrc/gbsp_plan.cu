@@ -867,13 +867,18 @@ struct gbsp_batch_s {
     int ku = 8, cw = 32, half = 0, idx_bytes = 2, big = 0;
     int p1_grid = 0;
     size_t p1_smem = 0;
-    int rows_grid = 0, rows_threads = 512;
-    size_t rows_smem = 0;
+    // Row launches: one per class of matrices that share a block size and a
+    // CTAs-per-SM count, so small rows keep the occupancy they have alone.
+    struct RowsClass {
+        int nt = 0, grid = 0, begin = 0, end = 0;  // descriptors [begin, end) in queue order
+        size_t smem = 0;
+    };
+    std::vector<RowsClass> classes;
     gbsp::P1Args* d_p1 = nullptr;
     long* d_p1_begin = nullptr;
     gbsp::RowsBatch* d_rows = nullptr;
-    long* d_row_begin = nullptr;
-    unsigned long long* d_queue = nullptr;  // [0] pass 1, [1] rows
+    long* d_row_begin = nullptr;            // per class: count+1 prefix entries from 0
+    unsigned long long* d_queue = nullptr;  // [0] pass 1, [1 + c] rows of class c
     int* d_err = nullptr;
     std::vector<void*> outs;
     std::vector<size_t> pitches;
@@ -939,12 +944,15 @@ int p1b_dispatch(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
 
 int batch_launch(gbsp_batch_s* b, cudaStream_t st) {
     if (!b->order.empty()) {
-        GB_CUDA(cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(unsigned long long), st));
+        GB_CUDA(cudaMemsetAsync(b->d_queue, 0, (1 + b->classes.size()) * sizeof(unsigned long long), st));
         int rc = p1b_dispatch(b, false, 0, st);
         if (rc) return rc;
-        gbsp::k_bluestein_rows_batch<512><<<b->rows_grid, b->rows_threads, b->rows_smem, st>>>(
-            b->d_rows, b->d_row_begin, (int)b->order.size(), b->d_queue + 1, b->d_err);
-        GB_CUDA(cudaGetLastError());
+        for (size_t c = 0; c < b->classes.size(); c++) {
+            const auto& k = b->classes[c];
+            gbsp::k_bluestein_rows_batch<512><<<k.grid, k.nt, k.smem, st>>>(
+                b->d_rows + k.begin, b->d_row_begin + k.begin + c, k.end - k.begin, b->d_queue + 1 + c, b->d_err);
+            GB_CUDA(cudaGetLastError());
+        }
     }
     for (int m : b->separate) {
         int rc = gbsp_execute(b->plans[m], b->outs[m], b->pitches[m], st);
@@ -1010,11 +1018,12 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
             return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: rows too large for the pass-1 table");
         }
     }
-    // one plan per matrix with the common shape and a 512-thread row block
+    // one plan per matrix with the common pass-1 shape; row blocks of 256 or
+    // 512 threads (the planner's automatic choice)
     gbsp_options o = opts ? *opts : gbsp_options{};
     o.u_tile = 0;
     o.index_bytes = b->idx_bytes;
-    o.rows_threads = b->rows_threads;
+    o.rows_threads = 0;
     o.row_table_mode = b->half ? 2 : 1;
     for (int& r : o.radix) r = 0;  // lengths differ across the batch: auto radices
     const int force[3] = {b->ku, b->cw, b->half};
@@ -1033,55 +1042,81 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
         free_batch(b);
         return rc;
     }
-    // queue order: single-channel matrices by decreasing channel length
-    for (int i = 0; i < count; i++) (b->plans[i]->K == 1 ? b->order : b->separate).push_back(i);
-    std::stable_sort(b->order.begin(), b->order.end(),
-                     [&](int x, int y) { return b->plans[x]->Lp > b->plans[y]->Lp; });
-    b->rows_smem = 0;
-    for (int m : b->order) {
-        b->rows_smem = std::max(b->rows_smem, rows_smem_bytes(b->plans[m]->fd));
+    // Single-channel matrices go through the queues, grouped into classes of
+    // (block size, CTAs per SM), classes with the longest rows first, and by
+    // decreasing channel length inside a class.
+    auto kern = gbsp::k_bluestein_rows_batch<512>;
+    if ((rc = allow_full_smem(kern))) {
+        free_batch(b);
+        return rc;
     }
-    const int n = (int)b->order.size();
-    if (n > 0) {
-        if (b->rows_smem + 1024 > smem_cap) {
-            free_batch(b);
-            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: batch row buffer exceeds shared memory");
+    std::vector<int> per_sm(count, 0);
+    for (int i = 0; i < count; i++) {
+        const gbsp_plan_s* p = b->plans[i];
+        if (p->K != 1 || p->rows_threads > 512) {
+            b->separate.push_back(i);
+            continue;
         }
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[i], kern, p->rows_threads,
+                                                          rows_smem_bytes(p->fd)) != cudaSuccess ||
+            per_sm[i] < 1) {
+            free_batch(b);
+            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: batched row kernel does not fit");
+        }
+        b->order.push_back(i);
+    }
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) {
+        const gbsp_plan_s *px = b->plans[x], *py = b->plans[y];
+        if (per_sm[x] != per_sm[y]) return per_sm[x] < per_sm[y];
+        if (px->rows_threads != py->rows_threads) return px->rows_threads > py->rows_threads;
+        return px->Lp > py->Lp;
+    });
+    const int n = (int)b->order.size();
+    for (int k = 0; k < n; k++) {
+        const gbsp_plan_s* p = b->plans[b->order[k]];
+        const int m = b->order[k];
+        if (b->classes.empty() || per_sm[b->order[k - 1]] != per_sm[m] ||
+            b->plans[b->order[k - 1]]->rows_threads != p->rows_threads) {
+            gbsp_batch_s::RowsClass c;
+            c.nt = p->rows_threads;
+            c.grid = per_sm[m] * sms;
+            c.begin = k;
+            b->classes.push_back(c);
+        }
+        b->classes.back().end = k + 1;
+        b->classes.back().smem = std::max(b->classes.back().smem, rows_smem_bytes(p->fd));
+    }
+    const int ncls = (int)b->classes.size();
+    if (n > 0) {
         if ((rc = p1b_dispatch(b, true, sms, st)) ||
             (rc = batch_alloc(b, (void**)&b->d_p1, sizeof(gbsp::P1Args) * n)) ||
             (rc = batch_alloc(b, (void**)&b->d_p1_begin, sizeof(long) * (n + 1))) ||
             (rc = batch_alloc(b, (void**)&b->d_rows, sizeof(gbsp::RowsBatch) * n)) ||
-            (rc = batch_alloc(b, (void**)&b->d_row_begin, sizeof(long) * (n + 1)))) {
+            (rc = batch_alloc(b, (void**)&b->d_row_begin, sizeof(long) * (n + ncls)))) {
             free_batch(b);
             return rc;
         }
-        auto kern = gbsp::k_bluestein_rows_batch<512>;
-        int nb = 0;
-        if (allow_full_smem(kern) != GBSP_OK ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, b->rows_threads, b->rows_smem) != cudaSuccess ||
-            nb < 1) {
-            free_batch(b);
-            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: batched row kernel does not fit");
-        }
-        b->rows_grid = nb * sms;
-        // work-queue prefix sums
+        // work-queue prefix sums (pass 1 over the whole queue, rows per class)
         std::vector<gbsp::P1Args> p1(n);
-        std::vector<long> p1b(n + 1, 0), rb(n + 1, 0);
+        std::vector<long> p1b(n + 1, 0), rb;
         const int ublk = 32 * b->ku;
         for (int k = 0; k < n; k++) {
             const gbsp_plan_s* p = b->plans[b->order[k]];
             p1[k] = p1_args(p, 0, p->half_rows, p->d_S, p->s_pitch, p->d_post);
             p1b[k + 1] = p1b[k] + (long)((p->half_rows + ublk - 1) / ublk) * ((p->s_cols + p->p1_cw - 1) / p->p1_cw);
-            rb[k + 1] = rb[k] + p->half_rows;
+        }
+        for (const auto& c : b->classes) {
+            rb.push_back(0);
+            for (int k = c.begin; k < c.end; k++) rb.push_back(rb.back() + b->plans[b->order[k]]->half_rows);
         }
         if (cudaMemcpy(b->d_p1, p1.data(), sizeof(gbsp::P1Args) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(b->d_p1_begin, p1b.data(), sizeof(long) * (n + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(b->d_row_begin, rb.data(), sizeof(long) * (n + 1), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaMemcpy(b->d_row_begin, rb.data(), sizeof(long) * rb.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
             free_batch(b);
             return set_error(GBSP_ERR_CUDA, "gbsp_batch_create: descriptor upload failed");
         }
     }
-    if ((rc = batch_alloc(b, (void**)&b->d_queue, 2 * sizeof(unsigned long long))) ||
+    if ((rc = batch_alloc(b, (void**)&b->d_queue, (1 + ncls) * sizeof(unsigned long long))) ||
         (rc = batch_alloc(b, (void**)&b->d_err, sizeof(int)))) {
         free_batch(b);
         return rc;

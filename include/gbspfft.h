@@ -187,10 +187,13 @@ int gbsp_plan_error_flags(gbsp_plan_t plan, int* flags);
  * (src/main.cu:249-311).  The reference has no batch entry point.
  *
  * gbsp_batch_create builds one sub-plan per matrix (same tables as
- * gbsp_plan_create, with one pass-1 shape and a 512-thread row block common
- * to the batch; explicit radices in opts are ignored).  Matrices whose
- * convolution needs several channels (thread-block clusters) run after the
- * batched launches through their own sub-plan.  Outputs are bound once with
+ * gbsp_plan_create, with one pass-1 shape common to the batch; opts'
+ * u_tile, rows_threads and radix are ignored: each matrix gets the
+ * planner's automatic radices and row block).  Pass 1 of all matrices is one
+ * launch; the Bluestein rows are one launch per class of matrices sharing a
+ * block size and CTAs-per-SM count.  Matrices whose convolution needs
+ * several channels (thread-block clusters) run after the batched launches
+ * through their own sub-plan.  Outputs are bound once with
  * gbsp_batch_set_outputs (same rules as gbsp_execute's d_out / out_pitch);
  * gbsp_batch_execute then enqueues the whole batch on `stream`.
  * gbsp_batch_graph_launch does the same through a CUDA graph captured on

@@ -73,7 +73,7 @@ def test_batch_matches_single_plans(cuda, policy):
     mats = mixed_batch(24, seed=11 + policy)
     outs, infos = run_batch(mats, length_policy=policy)
     for coo, got, info in zip(mats, outs, infos):
-        assert info["rows_threads"] == 512 and info["channels"] == 1
+        assert info["rows_threads"] in (256, 512) and info["channels"] == 1
         want = single_plan_output(coo, info, length_policy=policy)
         assert np.array_equal(got, want), f"{coo.rows}x{coo.cols} differs from its single plan"
         check_oracle(coo, got)
