@@ -22,6 +22,11 @@ GBSP_ERR_IO = 5
 GBSP_ERR_NOT_BUILT = 6
 GBSP_LEN_3SMOOTH = 3
 GBSP_LEN_7SMOOTH = 7
+GBSP_PLANNER_MODEL = 0
+GBSP_PLANNER_LEARNED = 1
+GBSP_N_PASS1_SHAPES = 6
+GBSP_N_FEATURES = 36
+GBSP_MLP_HIDDEN = 64
 
 # Every symbol include/gbspfft.h declares; tests check the library exports them.
 EXPORTED = (
@@ -30,7 +35,8 @@ EXPORTED = (
     "gbsp_plan_destroy", "gbsp_execute", "gbsp_execute_profiled", "gbsp_column_sums",
     "gbsp_plan_error_flags", "gbsp_execute_noalloc", "gbsp_batch_create", "gbsp_batch_set_outputs",
     "gbsp_batch_execute", "gbsp_batch_graph_launch", "gbsp_batch_plan_info", "gbsp_batch_error_flags",
-    "gbsp_batch_destroy",
+    "gbsp_batch_destroy", "gbsp_plan_candidates", "gbsp_plan_features", "gbsp_autotune", "gbsp_mlp_param_count",
+    "gbsp_mlp_forward", "gbsp_mlp_work_floats", "gbsp_mlp_backward", "gbsp_mlp_adam", "gbsp_cost_model_set",
 )
 
 
@@ -44,8 +50,13 @@ class GbspOptions(C.Structure):
         ("rows_threads", C.c_int),
         ("row_table_mode", C.c_int),
         ("radix", C.c_int * 8),
-        ("reserved", C.c_int * 4),
+        ("pass1_shape", C.c_int),
+        ("planner", C.c_int),
+        ("reserved", C.c_int * 2),
     ]
+
+    def radices(self) -> tuple:
+        return tuple(r for r in self.radix if r > 0)
 
 
 class GbspPlanInfo(C.Structure):
@@ -55,7 +66,7 @@ class GbspPlanInfo(C.Structure):
         ("n_stages", C.c_int), ("radix", C.c_int * 16), ("output_cols", C.c_int),
         ("output_pitch", C.c_int), ("half_rows", C.c_int), ("u_tile", C.c_int),
         ("index_bytes", C.c_int), ("row_table_mode", C.c_int), ("rows_threads", C.c_int),
-        ("device_bytes", C.c_size_t),
+        ("device_bytes", C.c_size_t), ("pass1_shape", C.c_int), ("planner", C.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -70,6 +81,10 @@ class GbspMatrix(C.Structure):
         ("col_ptr", C.POINTER(C.c_int)), ("row_idx", C.POINTER(C.c_int)),
         ("sparse_cols", C.POINTER(C.c_int)),
     ]
+
+
+class GbspTuneEntry(C.Structure):
+    _fields_ = [("opts", GbspOptions), ("ms_pass1", C.c_float), ("ms_rows", C.c_float)]
 
 
 class GbspError(RuntimeError):
@@ -119,8 +134,22 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbsp_batch_plan_info.argtypes = [vp, i32, C.POINTER(GbspPlanInfo)]
     lib.gbsp_batch_error_flags.argtypes = [vp, ip]
     lib.gbsp_batch_destroy.argtypes = [vp]
+    op = C.POINTER(GbspOptions)
+    fp = C.POINTER(C.c_float)
+    lib.gbsp_plan_candidates.argtypes = [i32, i32, op, i32, op, i32, ip, ip]
+    lib.gbsp_plan_features.argtypes = [i32, i32, i32, i32, ip, op, fp]
+    lib.gbsp_autotune.argtypes = [i32, i32, i32, i32, ip, ip, ip, op, i32, i32, vp, op, C.POINTER(GbspTuneEntry),
+                                  i32, ip, ip]
+    lib.gbsp_mlp_param_count.argtypes = [i32]
+    lib.gbsp_mlp_param_count.restype = C.c_size_t
+    lib.gbsp_mlp_work_floats.argtypes = [i32]
+    lib.gbsp_mlp_work_floats.restype = C.c_size_t
+    lib.gbsp_mlp_forward.argtypes = [vp, i32, vp, i32, vp, vp]
+    lib.gbsp_mlp_backward.argtypes = [vp, i32, vp, vp, i32, vp, vp, vp, vp]
+    lib.gbsp_mlp_adam.argtypes = [vp, vp, vp, vp, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp]
+    lib.gbsp_cost_model_set.argtypes = [fp, i32, fp, fp]
     for name in EXPORTED:
-        if name not in ("gbsp_status_string", "gbsp_free"):
+        if name not in ("gbsp_status_string", "gbsp_free", "gbsp_mlp_param_count", "gbsp_mlp_work_floats"):
             getattr(lib, name).restype = i32
     _lib = lib
     return lib

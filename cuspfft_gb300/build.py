@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               f"-I{INCLUDE}", f"-I{CSRC}"]
 
-LIB_SOURCES = ["gbsp_plan.cu", "gbsp_host.cpp", "sparse_fft_api.cu"]
+LIB_SOURCES = ["gbsp_plan.cu", "gbsp_planner.cu", "gbsp_mlp.cu", "gbsp_host.cpp", "sparse_fft_api.cu"]
 CLI_SOURCES = ["cli_main.cpp"]
 
 

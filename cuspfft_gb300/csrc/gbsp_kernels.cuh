@@ -9,37 +9,11 @@
 #pragma once
 #include <cooperative_groups.h>
 #include "gbsp_fft.cuh"
+#include "gbsp_layout.h"
 
 namespace cg = cooperative_groups;
 
 namespace gbsp {
-
-constexpr int MAX_STAGES = 16;
-constexpr int MAX_CHANNELS = 8;
-constexpr int P1_THREADS = 512;     // k_twiddle_sum block size
-constexpr int P1_WARPS = P1_THREADS / 32;
-constexpr int P1_RESEED = 4;        // exact table lookup every P1_RESEED rows
-// k_twiddle_sum shapes: KU Bluestein rows per lane (32*KU per work item) and
-// windows of cw consecutive columns cut into at most cw + P1_WARPS tasks
-__host__ __device__ constexpr int p1_vmax(int cw) { return cw + P1_WARPS; }
-__host__ __device__ constexpr int p1_pitch(int cw) { return p1_vmax(cw) + 1; }
-// shared memory before the twiddle table: result tile + per-warp nonzero data
-__host__ __device__ constexpr size_t p1_head_bytes(int ku, int cw) {
-    return (size_t)32 * ku * p1_pitch(cw) * 8 + (size_t)P1_WARPS * 32 * 16;
-}
-constexpr long long WAIT_LIMIT = 1LL << 26;  // bounded spin on an mbarrier (~seconds)
-constexpr int ERR_TIMEOUT = 1;              // bit set in the plan's error word
-
-struct FFTDesc {
-    int Lp;                     // channel FFT length
-    int nst;                    // stages
-    int R[MAX_STAGES];          // radix per stage
-    int m[MAX_STAGES];          // span per stage
-    uint32_t magic[MAX_STAGES]; // ceil(2^32 / m)
-    int twoff[MAX_STAGES];      // stage twiddle offset in the global table (q-major blocks)
-    int rest_base;              // first twiddle of stage 1 (stages >= 1 are staged in smem)
-    int rest_len;               // twiddles of stages >= 1
-};
 
 // ---------------------------------------------------------------------------
 // Exact integer phase helpers

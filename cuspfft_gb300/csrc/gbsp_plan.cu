@@ -19,8 +19,12 @@
 #include "gbspfft.h"
 #include "gbsp_internal.h"
 #include "gbsp_kernels.cuh"
+#include "gbsp_planner.h"
 
 using gbsp::set_error;
+using gbsp::rows_smem_bytes;
+using gbsp::fft_tw_count;
+using gbsp::max_radix_for;
 
 struct gbsp_plan_s {
     int device = 0;
@@ -30,6 +34,8 @@ struct gbsp_plan_s {
     int half_rows = 0, u_tile = 0, out_cols = 0, out_pitch = 0;
     int idx_bytes = 2, tab_half = 0, big = 0, kahan_min = 64, ntab = 0;
     int p1_ku = 8, p1_cw = 32;       // pass-1 rows per lane (x32 per item) and window width
+    int p1_shape = 1;                // 1-based index of (p1_ku, p1_cw, tab_half) in the shape table
+    int planner = GBSP_PLANNER_MODEL;
     uint32_t rows_magic = 0;
     void* d_row_idx = nullptr;       // nnz, u16 or u32, column order
     uint8_t* d_win_slot0 = nullptr;  // pass-1 windows: first tile column of each column
@@ -96,144 +102,6 @@ void free_plan(gbsp_plan_s* p) {
 }
 
 inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
-
-// Stage descriptor for a given radix sequence (product must be Lp).
-int build_fft_desc(int Lp, const std::vector<int>& rs, gbsp::FFTDesc* fd) {
-    if ((int)rs.size() > gbsp::MAX_STAGES || rs.empty()) return GBSP_ERR_UNSUPPORTED;
-    long prod = 1;
-    for (int r : rs) {
-        if (!gbsp::radix_supported(r)) return GBSP_ERR_UNSUPPORTED;
-        prod *= r;
-    }
-    if (prod != Lp) return GBSP_ERR_UNSUPPORTED;
-    fd->Lp = Lp;
-    fd->nst = (int)rs.size();
-    int l = 1, off = 0;
-    for (int s = 0; s < fd->nst; s++) {
-        const int R = rs[s];
-        const int m = Lp / (l * R);
-        fd->R[s] = R;
-        fd->m[s] = m;
-        // divisor of the stage's thread -> butterfly mapping (see fft_stage)
-        const int lcount = Lp / (R * m);
-        const int div = (m == 1) ? 0 : (gbsp::stage_j_fastest(R, m, lcount) ? lcount : m);
-        fd->magic[s] = (div <= 1) ? 0u : (uint32_t)(((1ull << 32) + (uint64_t)div - 1) / (uint64_t)div);
-        fd->twoff[s] = off;
-        off += (R - 1) * m;
-        l *= R;
-    }
-    fd->rest_base = (fd->R[0] - 1) * fd->m[0];
-    fd->rest_len = off - fd->rest_base;
-    return GBSP_OK;
-}
-
-int fft_tw_count(const gbsp::FFTDesc& fd) { return fd.rest_base + fd.rest_len; }
-
-size_t rows_smem_bytes(const gbsp::FFTDesc& fd) {
-    return ((size_t)fd.Lp + (size_t)fd.rest_len) * sizeof(float2);
-}
-
-// ---- radix planning -------------------------------------------------------
-// Every multiset of supported radices whose product is the channel length
-// (at most 7 stages) is ordered even radices first, odd radices last (an odd
-// radix at span 1 keeps the last stage free of bank conflicts) and scored by
-// a model fitted to GB300 measurements of the row kernel: a stage costs
-// (rounds of the block over its butterflies) x radix, forward and inverse
-// stages twice, the fused middle stage 1.6 times, radices above 32 a little
-// more (register pressure), plus a fixed cost per stage; the row time is that
-// cost divided by the CTAs resident per SM (a 512-thread block at 128
-// registers fills an SM's register file, smaller blocks can pair up when
-// shared memory allows).  Block sizes 256 and 512 are considered; 1024 only
-// on request.  The tuner can override the choice by measurement.
-const int kRadices[] = {40, 35, 32, 28, 25, 24, 21, 20, 16, 15, 12, 9, 8, 7, 5, 4, 3, 2};
-
-void factorizations(int rem, int maxr, std::vector<int>& cur, std::vector<std::vector<int>>& out) {
-    if (rem == 1) {
-        if (!cur.empty()) out.push_back(cur);
-        return;
-    }
-    if ((int)cur.size() >= 7) return;
-    for (int r : kRadices) {
-        if (r > maxr || rem % r) continue;
-        cur.push_back(r);
-        factorizations(rem / r, r, cur, out);
-        cur.pop_back();
-    }
-}
-
-std::vector<int> order_radices(std::vector<int> rs) {
-    std::stable_sort(rs.begin(), rs.end(), [](int a, int b) {
-        const bool ea = (a % 2 == 0), eb = (b % 2 == 0);
-        if (ea != eb) return ea;
-        return a > b;
-    });
-    return rs;
-}
-
-// largest radix a block of the given maximum size can hold in registers
-inline int max_radix_for(int nt_max) { return nt_max > 512 ? gbsp::MAX_RADIX_NT1024 : gbsp::MAX_RADIX_NT512; }
-
-// SM limits the model uses (GB300: 228 KB shared memory, 64K registers, 2048 threads per SM)
-constexpr size_t kSmemPerSM = 233472;
-constexpr int kRegsPerSM = 65536;
-
-double rows_cost(const gbsp::FFTDesc& fd, int nt, size_t smem_per_cta) {
-    double cost = 0.0;
-    for (int s = 0; s < fd.nst; s++) {
-        const int R = fd.R[s], m = fd.m[s], nb = fd.Lp / R, l = nb / m;
-        const double rounds = std::ceil((double)nb / (double)nt);
-        double per = rounds * R * (R > 32 ? 1.1 : 1.0);
-        const bool strided = (m == 1 && R % 2 == 0) ||
-                             (m > 1 && m < 16 && l > 1 && !gbsp::stage_j_fastest(R, m, l));
-        if (strided) per *= 1.5;
-        cost += ((s == fd.nst - 1) ? 1.6 : 2.0) * per + 12.0;
-    }
-    const int regs = nt <= 512 ? 128 : 64;
-    int ctas = std::min({(int)(kSmemPerSM / (smem_per_cta + 1024)), 2048 / nt, kRegsPerSM / (nt * regs)});
-    ctas = std::max(ctas, 1);
-    return cost / ctas;
-}
-
-struct RadixPlan {
-    gbsp::FFTDesc fd{};
-    int nt = 0;
-    double cost = 1e300;
-};
-
-// Best radix sequence and block size for channel length Lp within the
-// shared-memory budget; returns false if nothing fits.
-bool plan_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt, RadixPlan* best) {
-    std::vector<std::vector<int>> cands;
-    if (radix_opt && radix_opt[0] > 0) {
-        std::vector<int> rs;
-        for (int i = 0; i < 8 && radix_opt[i] > 0; i++) rs.push_back(radix_opt[i]);
-        cands.push_back(rs);
-    } else {
-        std::vector<int> cur;
-        factorizations(Lp, 64, cur, cands);
-        for (auto& c : cands) c = order_radices(c);
-    }
-    bool found = false;
-    for (const auto& rs : cands) {
-        gbsp::FFTDesc fd{};
-        if (build_fft_desc(Lp, rs, &fd) != GBSP_OK) continue;
-        if (rows_smem_bytes(fd) > smem_cap) continue;
-        const int rmax = *std::max_element(rs.begin(), rs.end());
-        const int nt_hi = rmax > max_radix_for(1024) ? 512 : 1024;
-        if (rmax > max_radix_for(512)) continue;
-        for (int nt : {256, 512, 1024, nt_opt}) {
-            if (nt <= 0 || nt > nt_hi || (nt_opt > 0 && nt != nt_opt) || (nt_opt == 0 && nt == 1024)) continue;
-            const double c = rows_cost(fd, nt, rows_smem_bytes(fd));
-            if (c < best->cost) {
-                best->cost = c;
-                best->fd = fd;
-                best->nt = nt;
-                found = true;
-            }
-        }
-    }
-    return found;
-}
 
 template <typename IDX, bool HALF, bool BIG, int KU>
 int p1_prepare(gbsp_plan_s* p, int sms) {
@@ -432,83 +300,93 @@ int validate_csc(int rows, int cols, int n_active, int nnz, const int* col_ptr,
     return GBSP_OK;
 }
 
-// force_p1: {ku, cw, half} imposes the pass-1 shape (batches need one shape
-// for all their matrices); nullptr chooses it from the shared-memory budget.
+// Learned planner: the cost model scores every tuning candidate of the
+// matrix and the cheapest prediction fills in o's radices, row block and
+// pass-1 shape.  The spectrum does not depend on the choice.
+int learned_choice(const gbsp_plan_s* p, const int* col_ptr, size_t smem_cap, gbsp_options* o) {
+    if (!gbsp::cost_model_loaded(gbsp::N_FEATURES))
+        return set_error(GBSP_ERR_INVALID, "planner: no cost model installed (gbsp_cost_model_set)");
+    std::vector<gbsp_options> cands;
+    int nr = 0, np = 0;
+    gbsp_options base = *o;
+    base.planner = GBSP_PLANNER_MODEL;
+    if (int rc = gbsp::enumerate_candidates(p->rows, p->cols, &base, smem_cap, 8, &cands, &nr, &np)) return rc;
+    std::vector<float> feats(cands.size() * gbsp::N_FEATURES), pred(cands.size());
+    for (size_t i = 0; i < cands.size(); i++)
+        if (int rc = gbsp::plan_features(p->rows, p->cols, p->n_active, p->nnz, col_ptr, &cands[i], smem_cap,
+                                         feats.data() + i * gbsp::N_FEATURES))
+            return rc;
+    if (int rc = gbsp::cost_model_predict(feats.data(), (int)cands.size(), pred.data())) return rc;
+    const size_t best = std::min_element(pred.begin(), pred.end()) - pred.begin();
+    std::memcpy(o->radix, cands[best].radix, sizeof(o->radix));
+    o->rows_threads = cands[best].rows_threads;
+    o->pass1_shape = cands[best].pass1_shape;
+    return GBSP_OK;
+}
+
+// force_p1: 1-based pass-1 shape imposed by a batch (one shape for all its
+// matrices); 0 leaves the choice to the options.
 int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int* sparse_cols,
-               const gbsp_options* o, cudaStream_t st, const int* force_p1 = nullptr) {
-    const int policy = (o && o->length_policy) ? o->length_policy : GBSP_LEN_3SMOOTH;
-    if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH)
-        return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: length_policy must be 3 or 7");
+               const gbsp_options* o_in, cudaStream_t st, int force_p1 = 0) {
+    gbsp_options o = o_in ? *o_in : gbsp_options{};
+    if (force_p1) o.pass1_shape = force_p1;
     GB_CUDA(cudaGetDevice(&p->device));
     cudaDeviceProp prop;
     GB_CUDA(cudaGetDeviceProperties(&prop, p->device));
     const size_t smem_cap = prop.sharedMemPerBlockOptin;
     const int sms = prop.multiProcessorCount;
+    const int tmode = o.row_table_mode;
+    if (tmode < 0 || tmode > 2) return set_error(GBSP_ERR_INVALID, "row_table_mode must be 0, 1 or 2");
+    if (o.pass1_shape < 0 || o.pass1_shape > gbsp::N_P1_SHAPES)
+        return set_error(GBSP_ERR_INVALID, "pass1_shape must be 0 (auto) or 1.." + std::to_string(gbsp::N_P1_SHAPES));
+    if (o.planner != GBSP_PLANNER_MODEL && o.planner != GBSP_PLANNER_LEARNED)
+        return set_error(GBSP_ERR_INVALID, "planner must be GBSP_PLANNER_MODEL or GBSP_PLANNER_LEARNED");
+    int rc = GBSP_OK;
+    if (o.planner == GBSP_PLANNER_LEARNED && (rc = learned_choice(p, col_ptr, smem_cap, &o))) return rc;
+    p->planner = o.planner;
 
-    // ---- lengths and channel split
-    long L = gbsp::next_smooth(2L * p->cols - 1, policy);
-    if (L < 2) L = 2;
-    if (L > (1L << 28)) return set_error(GBSP_ERR_UNSUPPORTED, "fft_len too large");
-    p->L = (int)L;
-    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 24000;
-    const int nt_opt = o ? o->rows_threads : 0;
-    if (nt_opt < 0 || nt_opt % 32 || nt_opt > 1024)
-        return set_error(GBSP_ERR_INVALID, "rows_threads must be 0 or a multiple of 32 up to 1024");
-    p->K = 0;
-    for (int k = 1; k <= gbsp::MAX_CHANNELS && !p->K; k++) {
-        if (L % k || L / k > maxLp || L / k < 2) continue;
-        RadixPlan rp;
-        if (!plan_radices((int)(L / k), smem_cap, o ? o->radix : nullptr, nt_opt, &rp)) continue;
-        p->K = k;
-        p->fd = rp.fd;
-        p->rows_threads = rp.nt;
-    }
-    if (p->K == 0)
-        return set_error(GBSP_ERR_UNSUPPORTED,
-                         "fft_len " + std::to_string(L) + " does not split into <= 8 channels of <= " +
-                             std::to_string(maxLp) + " that fit in shared memory");
-    p->Lp = (int)(L / p->K);
+    // ---- lengths, channel split, radices and row block
+    gbsp::ChannelSplit sp;
+    if ((rc = gbsp::split_channels(p->cols, &o, smem_cap, &sp))) return rc;
+    p->L = sp.L;
+    p->K = sp.K;
+    p->Lp = sp.Lp;
+    p->fd = sp.ranked[0].fd;
+    p->rows_threads = sp.ranked[0].nt;
 
     p->half_rows = p->rows / 2 + 1;
     p->out_cols = p->cols / 2 + 1;
     p->out_pitch = (p->out_cols + 3) / 4 * 4;
-    p->u_tile = (o && o->u_tile > 0) ? std::min(o->u_tile, p->half_rows) : p->half_rows;
-    p->kahan_min = (o && o->kahan_min_degree != 0) ? o->kahan_min_degree : 64;
+    p->u_tile = (o.u_tile > 0) ? std::min(o.u_tile, p->half_rows) : p->half_rows;
+    p->kahan_min = (o.kahan_min_degree != 0) ? o.kahan_min_degree : 64;
     if (p->kahan_min < 0) p->kahan_min = 0;  // 0 disables compensation in the kernel
-    int ib = (o && o->index_bytes) ? o->index_bytes : ((p->rows <= 65536 && p->cols <= 65536) ? 2 : 4);
+    int ib = o.index_bytes ? o.index_bytes : ((p->rows <= 65536 && p->cols <= 65536) ? 2 : 4);
     if (ib != 2 && ib != 4) return set_error(GBSP_ERR_INVALID, "index_bytes must be 2 or 4");
     if (ib == 2 && p->rows > 65536) return set_error(GBSP_ERR_INVALID, "rows > 65536 need 4-byte indices");
     p->idx_bytes = ib;
     p->big = p->rows > 65535;
     p->rows_magic = (p->rows >= 2) ? (uint32_t)(((1ull << 32) + (uint64_t)p->rows - 1) / (uint64_t)p->rows) : 0u;
 
-    // ---- pass-1 configuration: result tile + twiddle table in shared memory.
-    // Preference order: 256-row items with 32-column windows, full table, then
-    // half table; then 128-row items with 64- or 32-column windows.
-    const int tmode = o ? o->row_table_mode : 0;
-    if (tmode < 0 || tmode > 2) return set_error(GBSP_ERR_INVALID, "row_table_mode must be 0, 1 or 2");
+    // ---- pass-1 configuration: result tile + twiddle table in shared memory
     {
-        struct Shape { int ku, cw, half; };
-        const Shape shapes[] = {{8, 32, 0}, {8, 32, 1}, {4, 64, 0}, {4, 32, 0}, {4, 64, 1}, {4, 32, 1}};
-        bool ok = false;
-        for (const Shape& sh : shapes) {
-            if ((tmode == 1 && sh.half) || (tmode == 2 && !sh.half)) continue;
-            if (force_p1 && (sh.ku != force_p1[0] || sh.cw != force_p1[1] || sh.half != force_p1[2])) continue;
-            const size_t ntab = sh.half ? (size_t)(p->rows / 2 + 1) : (size_t)p->rows;
-            const size_t bytes = gbsp::p1_head_bytes(sh.ku, sh.cw) + ntab * sizeof(float2);
-            if (bytes + 1024 > smem_cap) continue;  // static shared variables
-            p->p1_ku = sh.ku;
-            p->p1_cw = sh.cw;
-            p->tab_half = sh.half;
-            p->ntab = (int)ntab;
-            p->p1_smem = bytes;
-            ok = true;
-            break;
+        const std::vector<int> fit = gbsp::fitting_p1_shapes(p->rows, smem_cap, tmode);
+        int idx = fit.empty() ? -1 : fit[0];
+        if (o.pass1_shape > 0) {
+            idx = o.pass1_shape - 1;
+            if (std::find(fit.begin(), fit.end(), idx) == fit.end())
+                return set_error(GBSP_ERR_UNSUPPORTED, "pass1_shape " + std::to_string(o.pass1_shape) +
+                                                           " does not fit this matrix or row_table_mode");
         }
-        if (!ok) return set_error(GBSP_ERR_UNSUPPORTED, "rows too large for a shared-memory twiddle table");
+        if (idx < 0) return set_error(GBSP_ERR_UNSUPPORTED, "rows too large for a shared-memory twiddle table");
+        const gbsp::P1Shape& sh = gbsp::kP1Shapes[idx];
+        p->p1_shape = idx + 1;
+        p->p1_ku = sh.ku;
+        p->p1_cw = sh.cw;
+        p->tab_half = sh.half;
+        p->ntab = sh.half ? p->rows / 2 + 1 : p->rows;
+        p->p1_smem = gbsp::p1_smem_bytes(sh, p->rows);
     }
-    int rc = p1_dispatch(p, true, sms, 0, 0, nullptr, 0, nullptr, st);
-    if (rc) return rc;
+    if ((rc = p1_dispatch(p, true, sms, 0, 0, nullptr, 0, nullptr, st))) return rc;
 
     // ---- row-kernel configuration
     p->rows_smem = rows_smem_bytes(p->fd);
@@ -678,6 +556,8 @@ int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
     info->row_table_mode = p->tab_half;
     info->rows_threads = p->rows_threads;
     info->device_bytes = p->device_bytes;
+    info->pass1_shape = p->p1_shape;
+    info->planner = p->planner;
     return GBSP_OK;
 }
 
@@ -864,7 +744,7 @@ struct gbsp_batch_s {
     std::vector<gbsp_plan_s*> plans;
     std::vector<int> order;      // queue order (batched matrices, costliest rows first)
     std::vector<int> separate;   // matrices that run through their own plan
-    int ku = 8, cw = 32, half = 0, idx_bytes = 2, big = 0;
+    int p1_shape = 1, ku = 8, cw = 32, half = 0, idx_bytes = 2, big = 0;
     int p1_grid = 0;
     size_t p1_smem = 0;
     // Row launches: one per class of matrices that share a block size and a
@@ -997,26 +877,21 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
     b->idx_bytes = u32 ? 4 : 2;
     b->big = max_rows > 65535;
     {
-        struct Shape { int ku, cw, half; };
-        const Shape shapes[] = {{8, 32, 0}, {8, 32, 1}, {4, 64, 0}, {4, 32, 0}, {4, 64, 1}, {4, 32, 1}};
-        bool ok = false;
         const int tmode = opts ? opts->row_table_mode : 0;
-        for (const Shape& sh : shapes) {
-            if ((tmode == 1 && sh.half) || (tmode == 2 && !sh.half)) continue;
-            const size_t ntab = sh.half ? (size_t)(max_rows / 2 + 1) : (size_t)max_rows;
-            const size_t bytes = gbsp::p1_head_bytes(sh.ku, sh.cw) + ntab * sizeof(float2);
-            if (bytes + 1024 > smem_cap) continue;
-            b->ku = sh.ku;
-            b->cw = sh.cw;
-            b->half = sh.half;
-            b->p1_smem = bytes;
-            ok = true;
-            break;
+        std::vector<int> fit = gbsp::fitting_p1_shapes(max_rows, smem_cap, tmode);
+        if (opts && opts->pass1_shape > 0) {
+            const int want = opts->pass1_shape - 1;
+            fit.erase(std::remove_if(fit.begin(), fit.end(), [&](int i) { return i != want; }), fit.end());
         }
-        if (!ok) {
+        if (fit.empty()) {
             free_batch(b);
-            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: rows too large for the pass-1 table");
+            return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: no pass-1 shape fits the largest matrix");
         }
+        b->p1_shape = fit[0] + 1;
+        b->ku = gbsp::kP1Shapes[fit[0]].ku;
+        b->cw = gbsp::kP1Shapes[fit[0]].cw;
+        b->half = gbsp::kP1Shapes[fit[0]].half;
+        b->p1_smem = gbsp::p1_smem_bytes(gbsp::kP1Shapes[fit[0]], max_rows);
     }
     // one plan per matrix with the common pass-1 shape; row blocks of 256 or
     // 512 threads (the planner's automatic choice)
@@ -1024,9 +899,8 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
     o.u_tile = 0;
     o.index_bytes = b->idx_bytes;
     o.rows_threads = 0;
-    o.row_table_mode = b->half ? 2 : 1;
-    for (int& r : o.radix) r = 0;  // lengths differ across the batch: auto radices
-    const int force[3] = {b->ku, b->cw, b->half};
+    o.row_table_mode = 0;
+    for (int& r : o.radix) r = 0;  // lengths differ across the batch: per-matrix radices
     b->plans.assign(count, nullptr);
     for (int i = 0; i < count && rc == GBSP_OK; i++) {
         gbsp_plan_s* p = new (std::nothrow) gbsp_plan_s();
@@ -1036,7 +910,7 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
         p->nnz = mats[i].nnz;
         p->n_active = mats[i].n_active;
         b->plans[i] = p;
-        rc = plan_build(p, mats[i].col_ptr, mats[i].row_idx, mats[i].sparse_cols, &o, st, force);
+        rc = plan_build(p, mats[i].col_ptr, mats[i].row_idx, mats[i].sparse_cols, &o, st, b->p1_shape);
     }
     if (rc) {
         free_batch(b);

@@ -1,0 +1,394 @@
+// gbsp_planner.cu -- host-side planning (no kernels): channel split, radix
+// sequences and row-block sizes ranked by an analytic model, pass-1 shapes,
+// tuning candidates and the feature vector of the learned cost model.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gbsp_fft.cuh"
+#include "gbsp_internal.h"
+#include "gbsp_planner.h"
+
+namespace gbsp {
+
+// Stage descriptor for a given radix sequence (product must be Lp).
+int build_fft_desc(int Lp, const std::vector<int>& rs, FFTDesc* fd) {
+    if ((int)rs.size() > MAX_STAGES || rs.empty()) return GBSP_ERR_UNSUPPORTED;
+    long prod = 1;
+    for (int r : rs) {
+        if (!radix_supported(r)) return GBSP_ERR_UNSUPPORTED;
+        prod *= r;
+    }
+    if (prod != Lp) return GBSP_ERR_UNSUPPORTED;
+    fd->Lp = Lp;
+    fd->nst = (int)rs.size();
+    int l = 1, off = 0;
+    for (int s = 0; s < fd->nst; s++) {
+        const int R = rs[s];
+        const int m = Lp / (l * R);
+        fd->R[s] = R;
+        fd->m[s] = m;
+        // divisor of the stage's thread -> butterfly mapping (see fft_stage)
+        const int lcount = Lp / (R * m);
+        const int div = (m == 1) ? 0 : (stage_j_fastest(R, m, lcount) ? lcount : m);
+        fd->magic[s] = (div <= 1) ? 0u : (uint32_t)(((1ull << 32) + (uint64_t)div - 1) / (uint64_t)div);
+        fd->twoff[s] = off;
+        off += (R - 1) * m;
+        l *= R;
+    }
+    fd->rest_base = (fd->R[0] - 1) * fd->m[0];
+    fd->rest_len = off - fd->rest_base;
+    return GBSP_OK;
+}
+
+int fft_tw_count(const FFTDesc& fd) { return fd.rest_base + fd.rest_len; }
+
+size_t rows_smem_bytes(const FFTDesc& fd) {
+    return ((size_t)fd.Lp + (size_t)fd.rest_len) * sizeof(float2);
+}
+
+// ---- radix planning -------------------------------------------------------
+// Every multiset of supported radices whose product is the channel length
+// (at most 7 stages) is ordered even radices first, odd radices last (an odd
+// radix at span 1 keeps the last stage free of bank conflicts) and scored by
+// a model fitted to GB300 measurements of the row kernel: a stage costs
+// (rounds of the block over its butterflies) x radix, forward and inverse
+// stages twice, the fused middle stage 1.6 times, radices above 32 a little
+// more (register pressure), plus a fixed cost per stage; the row time is that
+// cost divided by the CTAs resident per SM (a 512-thread block at 128
+// registers fills an SM's register file, smaller blocks can pair up when
+// shared memory allows).  Block sizes 256 and 512 are considered; 1024 only
+// on request.  The tuner can override the choice by measurement.
+static const int kRadices[] = {40, 35, 32, 28, 25, 24, 21, 20, 16, 15, 12, 9, 8, 7, 5, 4, 3, 2};
+
+static void factorizations(int rem, int maxr, std::vector<int>& cur, std::vector<std::vector<int>>& out) {
+    if (rem == 1) {
+        if (!cur.empty()) out.push_back(cur);
+        return;
+    }
+    if ((int)cur.size() >= 7) return;
+    for (int r : kRadices) {
+        if (r > maxr || rem % r) continue;
+        cur.push_back(r);
+        factorizations(rem / r, r, cur, out);
+        cur.pop_back();
+    }
+}
+
+static std::vector<int> order_radices(std::vector<int> rs) {
+    std::stable_sort(rs.begin(), rs.end(), [](int a, int b) {
+        const bool ea = (a % 2 == 0), eb = (b % 2 == 0);
+        if (ea != eb) return ea;
+        return a > b;
+    });
+    return rs;
+}
+
+// largest radix a block of the given maximum size can hold in registers
+int max_radix_for(int nt_max) { return nt_max > 512 ? MAX_RADIX_NT1024 : MAX_RADIX_NT512; }
+
+// SM limits the model uses (GB300: 228 KB shared memory, 64K registers, 2048 threads per SM)
+constexpr size_t kSmemPerSM = 233472;
+constexpr int kRegsPerSM = 65536;
+
+double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta) {
+    double cost = 0.0;
+    for (int s = 0; s < fd.nst; s++) {
+        const int R = fd.R[s], m = fd.m[s], nb = fd.Lp / R, l = nb / m;
+        const double rounds = std::ceil((double)nb / (double)nt);
+        double per = rounds * R * (R > 32 ? 1.1 : 1.0);
+        const bool strided = (m == 1 && R % 2 == 0) ||
+                             (m > 1 && m < 16 && l > 1 && !stage_j_fastest(R, m, l));
+        if (strided) per *= 1.5;
+        cost += ((s == fd.nst - 1) ? 1.6 : 2.0) * per + 12.0;
+    }
+    const int regs = nt <= 512 ? 128 : 64;
+    int ctas = std::min({(int)(kSmemPerSM / (smem_per_cta + 1024)), 2048 / nt, kRegsPerSM / (nt * regs)});
+    ctas = std::max(ctas, 1);
+    return cost / ctas;
+}
+
+std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt) {
+    std::vector<std::vector<int>> cands;
+    if (radix_opt && radix_opt[0] > 0) {
+        std::vector<int> rs;
+        for (int i = 0; i < 8 && radix_opt[i] > 0; i++) rs.push_back(radix_opt[i]);
+        cands.push_back(rs);
+    } else {
+        std::vector<int> cur;
+        factorizations(Lp, 64, cur, cands);
+        for (auto& c : cands) c = order_radices(c);
+    }
+    std::vector<RadixPlan> out;
+    for (const auto& rs : cands) {
+        FFTDesc fd{};
+        if (build_fft_desc(Lp, rs, &fd) != GBSP_OK) continue;
+        if (rows_smem_bytes(fd) > smem_cap) continue;
+        const int rmax = *std::max_element(rs.begin(), rs.end());
+        const int nt_hi = rmax > max_radix_for(1024) ? 512 : 1024;
+        if (rmax > max_radix_for(512)) continue;
+        for (int nt : {256, 512, 1024, nt_opt}) {
+            if (nt <= 0 || nt > nt_hi || (nt_opt > 0 && nt != nt_opt) || (nt_opt == 0 && nt == 1024)) continue;
+            if (nt_opt > 0 && !out.empty() && out.back().nt == nt && std::memcmp(&out.back().fd, &fd, sizeof(fd)) == 0)
+                continue;  // nt_opt listed twice
+            RadixPlan rp;
+            rp.fd = fd;
+            rp.nt = nt;
+            rp.cost = rows_cost(fd, nt, rows_smem_bytes(fd));
+            out.push_back(rp);
+        }
+    }
+    std::stable_sort(out.begin(), out.end(), [](const RadixPlan& a, const RadixPlan& b) { return a.cost < b.cost; });
+    return out;
+}
+
+int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSplit* out) {
+    const int policy = (o && o->length_policy) ? o->length_policy : GBSP_LEN_3SMOOTH;
+    if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH)
+        return set_error(GBSP_ERR_INVALID, "length_policy must be 3 or 7");
+    const int nt_opt = o ? o->rows_threads : 0;
+    if (nt_opt < 0 || nt_opt % 32 || nt_opt > 1024)
+        return set_error(GBSP_ERR_INVALID, "rows_threads must be 0 or a multiple of 32 up to 1024");
+    long L = next_smooth(2L * cols - 1, policy);
+    if (L < 2) L = 2;
+    if (L > (1L << 28)) return set_error(GBSP_ERR_UNSUPPORTED, "fft_len too large");
+    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 24000;
+    out->L = (int)L;
+    out->K = 0;
+    for (int k = 1; k <= MAX_CHANNELS; k++) {
+        if (L % k || L / k > maxLp || L / k < 2) continue;
+        auto ranked = rank_radices((int)(L / k), smem_cap, o ? o->radix : nullptr, nt_opt);
+        if (ranked.empty()) continue;
+        out->K = k;
+        out->Lp = (int)(L / k);
+        out->ranked = std::move(ranked);
+        return GBSP_OK;
+    }
+    return set_error(GBSP_ERR_UNSUPPORTED, "fft_len " + std::to_string(L) + " does not split into <= " +
+                                               std::to_string(MAX_CHANNELS) + " channels of <= " +
+                                               std::to_string(maxLp) + " that fit in shared memory");
+}
+
+// Preference order: 256-row items with 32-column windows, full table, then
+// half table; then 128-row items with 64- or 32-column windows.
+const P1Shape kP1Shapes[N_P1_SHAPES] = {{8, 32, 0}, {8, 32, 1}, {4, 64, 0}, {4, 32, 0}, {4, 64, 1}, {4, 32, 1}};
+
+size_t p1_smem_bytes(const P1Shape& sh, int rows) {
+    const size_t ntab = sh.half ? (size_t)(rows / 2 + 1) : (size_t)rows;
+    return p1_head_bytes(sh.ku, sh.cw) + ntab * 8;
+}
+
+std::vector<int> fitting_p1_shapes(int rows, size_t smem_cap, int table_mode) {
+    std::vector<int> out;
+    for (int i = 0; i < N_P1_SHAPES; i++) {
+        const P1Shape& sh = kP1Shapes[i];
+        if ((table_mode == 1 && sh.half) || (table_mode == 2 && !sh.half)) continue;
+        if (p1_smem_bytes(sh, rows) + 1024 > smem_cap) continue;  // + static shared variables
+        out.push_back(i);
+    }
+    return out;
+}
+
+size_t device_smem_cap() {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess && optin > 0)
+        return (size_t)optin;
+    cudaGetLastError();
+    return 232448;
+}
+
+int enumerate_candidates(int rows, int cols, const gbsp_options* base, size_t smem_cap, int max_rows,
+                         std::vector<gbsp_options>* out, int* n_rows, int* n_p1) {
+    if (rows < 1 || cols < 1 || max_rows < 1) return set_error(GBSP_ERR_INVALID, "enumerate_candidates: bad sizes");
+    gbsp_options o = base ? *base : gbsp_options{};
+    ChannelSplit sp;
+    if (int rc = split_channels(cols, &o, smem_cap, &sp)) return rc;
+    const int tmode = o.row_table_mode;
+    std::vector<int> shapes;
+    if (o.pass1_shape > 0) {
+        if (o.pass1_shape > N_P1_SHAPES) return set_error(GBSP_ERR_INVALID, "pass1_shape out of range");
+        shapes.push_back(o.pass1_shape - 1);
+    } else {
+        shapes = fitting_p1_shapes(rows, smem_cap, tmode);
+    }
+    if (shapes.empty()) return set_error(GBSP_ERR_UNSUPPORTED, "rows too large for a shared-memory twiddle table");
+    const int nr = std::min<int>(max_rows, (int)sp.ranked.size());
+    out->clear();
+    for (int i = 0; i < nr; i++) {
+        for (int j : shapes) {
+            gbsp_options c = o;
+            std::memset(c.radix, 0, sizeof(c.radix));
+            const FFTDesc& fd = sp.ranked[i].fd;
+            if (fd.nst > 8) return set_error(GBSP_ERR_UNSUPPORTED, "more than 8 radix stages");
+            for (int s = 0; s < fd.nst; s++) c.radix[s] = fd.R[s];
+            c.rows_threads = sp.ranked[i].nt;
+            c.pass1_shape = j + 1;
+            out->push_back(c);
+        }
+    }
+    *n_rows = nr;
+    *n_p1 = (int)shapes.size();
+    return GBSP_OK;
+}
+
+static int largest_prime_factor(int n) {
+    int best = 1;
+    for (int p = 2; (long)p * p <= n; p++)
+        while (n % p == 0) {
+            best = p;
+            n /= p;
+        }
+    return n > 1 ? std::max(best, n) : best;
+}
+
+static float lg2(double x) { return (float)std::log2(std::max(x, 1e-30)); }
+
+int plan_features(int rows, int cols, int n_active, int nnz, const int* col_ptr, const gbsp_options* cand,
+                  size_t smem_cap, float* f) {
+    if (!cand || !f || rows < 1 || cols < 1 || n_active < 0 || nnz < 0 || (n_active > 0 && !col_ptr))
+        return set_error(GBSP_ERR_INVALID, "plan_features: bad arguments");
+    ChannelSplit sp;
+    if (int rc = split_channels(cols, cand, smem_cap, &sp)) return rc;
+    const RadixPlan& rp = sp.ranked[0];  // radix and rows_threads of cand restrict the ranking to one choice
+    const int sh_idx = cand->pass1_shape - 1;
+    if (sh_idx < 0 || sh_idx >= N_P1_SHAPES) return set_error(GBSP_ERR_INVALID, "plan_features: pass1_shape unset");
+    const P1Shape& sh = kP1Shapes[sh_idx];
+    const int half_rows = rows / 2 + 1;
+    std::fill(f, f + N_FEATURES, 0.f);
+    // matrix
+    int maxdeg = 0;
+    double hist[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < n_active; j++) {
+        const int d = col_ptr[j + 1] - col_ptr[j];
+        maxdeg = std::max(maxdeg, d);
+        const int b = d <= 1 ? 0 : d <= 3 ? 1 : d <= 7 ? 2 : d <= 15 ? 3 : d <= 63 ? 4 : 5;
+        hist[b] += 1.0;
+    }
+    f[0] = lg2(rows);
+    f[1] = lg2(cols);
+    f[2] = lg2(nnz + 1.0);
+    f[3] = lg2(n_active + 1.0);
+    f[4] = lg2((nnz + 1.0) / ((double)rows * cols));
+    f[5] = lg2(largest_prime_factor(rows));
+    f[6] = lg2(largest_prime_factor(cols));
+    f[7] = lg2(sp.L);
+    f[8] = (float)sp.K;
+    f[9] = lg2(maxdeg + 1.0);
+    for (int b = 0; b < 6; b++) f[10 + b] = n_active ? (float)(hist[b] / n_active) : 0.f;
+    f[16] = lg2((double)half_rows * cols);
+    f[17] = lg2((double)nnz * half_rows + 1.0);
+    // row choice
+    const FFTDesc& fd = rp.fd;
+    int rmax = 0;
+    for (int s = 0; s < fd.nst; s++) rmax = std::max(rmax, fd.R[s]);
+    f[18] = rp.nt / 512.f;
+    f[19] = (float)fd.nst;
+    for (int s = 0; s < 4 && s < fd.nst; s++) f[20 + s] = lg2(fd.R[s]);
+    f[24] = lg2(rmax);
+    f[25] = lg2((double)rows_smem_bytes(fd));
+    const int regs = rp.nt <= 512 ? 128 : 64;
+    f[26] = (float)std::max(1, std::min({(int)(233472 / (rows_smem_bytes(fd) + 1024)), 2048 / rp.nt,
+                                         65536 / (rp.nt * regs)}));
+    f[27] = lg2(rp.cost);
+    // pass-1 shape
+    f[28 + sh_idx] = 1.f;
+    const int s_cols = (cols + 1) & ~1;
+    const double items = std::ceil(half_rows / (32.0 * sh.ku)) * std::ceil((double)s_cols / sh.cw);
+    f[34] = lg2(items);
+    f[35] = lg2((double)p1_smem_bytes(sh, rows));
+    return GBSP_OK;
+}
+
+}  // namespace gbsp
+
+using gbsp::set_error;
+
+extern "C" {
+
+int gbsp_plan_candidates(int rows, int cols, const gbsp_options* base, int max_rows_cands, gbsp_options* out,
+                         int cap, int* n_rows_cands, int* n_p1_cands) {
+    if (!n_rows_cands || !n_p1_cands || (cap > 0 && !out))
+        return set_error(GBSP_ERR_INVALID, "gbsp_plan_candidates: null argument");
+    std::vector<gbsp_options> c;
+    int nr = 0, np = 0;
+    if (int rc = gbsp::enumerate_candidates(rows, cols, base, gbsp::device_smem_cap(), max_rows_cands, &c, &nr, &np))
+        return rc;
+    *n_rows_cands = nr;
+    *n_p1_cands = np;
+    if ((int)c.size() > cap)
+        return set_error(GBSP_ERR_INVALID, "gbsp_plan_candidates: cap < " + std::to_string(c.size()));
+    std::copy(c.begin(), c.end(), out);
+    return GBSP_OK;
+}
+
+int gbsp_plan_features(int rows, int cols, int n_active, int nnz, const int* col_ptr, const gbsp_options* cand,
+                       float* out) {
+    return gbsp::plan_features(rows, cols, n_active, nnz, col_ptr, cand, gbsp::device_smem_cap(), out);
+}
+
+int gbsp_autotune(int rows, int cols, int n_active, int nnz, const int* col_ptr, const int* row_idx,
+                  const int* sparse_cols, const gbsp_options* base, int max_rows_cands, int reps, void* stream,
+                  gbsp_options* best, gbsp_tune_entry* entries, int cap, int* n_rows_cands, int* n_p1_cands) {
+    if (!best || !n_rows_cands || !n_p1_cands || reps < 1 || (cap > 0 && !entries))
+        return set_error(GBSP_ERR_INVALID, "gbsp_autotune: bad arguments");
+    gbsp_options b = base ? *base : gbsp_options{};
+    b.planner = GBSP_PLANNER_MODEL;
+    std::vector<gbsp_options> c;
+    int nr = 0, np = 0;
+    if (int rc = gbsp::enumerate_candidates(rows, cols, &b, gbsp::device_smem_cap(), max_rows_cands, &c, &nr, &np))
+        return rc;
+    *n_rows_cands = nr;
+    *n_p1_cands = np;
+    if (cap > 0 && (int)c.size() > cap)
+        return set_error(GBSP_ERR_INVALID, "gbsp_autotune: cap < " + std::to_string(c.size()));
+    const size_t pitch = (size_t)((cols / 2 + 1 + 3) / 4 * 4);
+    void* d_out = nullptr;
+    cudaError_t e = cudaMalloc(&d_out, (size_t)rows * pitch * 8);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(GBSP_ERR_ALLOC, std::string("gbsp_autotune: output buffer: ") + cudaGetErrorString(e));
+    }
+    std::vector<float> p1(np, INFINITY), rw(nr, INFINITY);
+    int rc = GBSP_OK;
+    const int T = std::max(nr, np);
+    for (int t = 0; t < T && rc == GBSP_OK; t++) {
+        const int i = t % nr, j = t % np;
+        gbsp_plan_t pl = nullptr;
+        rc = gbsp_plan_create(rows, cols, n_active, nnz, col_ptr, row_idx, sparse_cols, &c[(size_t)i * np + j], stream,
+                              &pl);
+        if (rc) break;
+        rc = gbsp_execute(pl, d_out, pitch, stream);  // warm-up
+        for (int r = 0; r < reps && rc == GBSP_OK; r++) {
+            float a = 0.f, q = 0.f;
+            rc = gbsp_execute_profiled(pl, d_out, pitch, stream, &a, &q);
+            p1[j] = std::min(p1[j], a);
+            rw[i] = std::min(rw[i], q);
+        }
+        gbsp_plan_destroy(pl);
+    }
+    cudaFree(d_out);
+    if (rc) return rc;
+    int bi = 0, bj = 0;
+    for (int i = 0; i < nr; i++)
+        for (int j = 0; j < np; j++) {
+            if (cap > 0) {
+                gbsp_tune_entry& en = entries[(size_t)i * np + j];
+                en.opts = c[(size_t)i * np + j];
+                en.ms_pass1 = p1[j];
+                en.ms_rows = rw[i];
+            }
+            if (p1[j] + rw[i] < p1[bj] + rw[bi]) {
+                bi = i;
+                bj = j;
+            }
+        }
+    *best = c[(size_t)bi * np + bj];
+    return GBSP_OK;
+}
+
+}  // extern "C"

@@ -14,7 +14,8 @@ from typing import Optional
 import numpy as np
 
 from . import _capi
-from ._capi import GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GbspMatrix, GbspOptions, GbspPlanInfo, check, load
+from ._capi import (GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GBSP_PLANNER_LEARNED, GBSP_PLANNER_MODEL, GbspMatrix,
+                    GbspOptions, GbspPlanInfo, check, load)
 
 
 @dataclass
@@ -107,24 +108,53 @@ def _stream_handle(stream) -> Optional[int]:
     return stream.cuda_stream
 
 
+def planner_code(planner) -> int:
+    """"model" (analytic, default) or "learned" (the installed MLP cost model;
+    the packaged model is installed on first use)."""
+    if planner in (None, "model", GBSP_PLANNER_MODEL):
+        return GBSP_PLANNER_MODEL
+    if planner in ("learned", GBSP_PLANNER_LEARNED):
+        from . import costmodel
+        costmodel.ensure_installed()
+        return GBSP_PLANNER_LEARNED
+    raise ValueError(f"unknown planner {planner!r}")
+
+
+def make_options(options: Optional[GbspOptions] = None, radix=None, planner=None, **fields) -> GbspOptions:
+    """GbspOptions from an existing one (e.g. an autotuner result) with the
+    given fields overriding; zero fields mean automatic."""
+    o = GbspOptions()
+    if options is not None:
+        C.memmove(C.byref(o), C.byref(options), C.sizeof(GbspOptions))
+    for k, v in fields.items():
+        if v:
+            setattr(o, k, int(v))
+    if radix:
+        for i in range(8):
+            o.radix[i] = int(radix[i]) if i < len(radix) else 0
+    if planner is not None or options is None:
+        o.planner = planner_code(planner)
+    return o
+
+
 class Plan:
     """One matrix's transform: tables and uploaded CSC live on the GPU until
     close().  execute() is the reference's timed tile loop."""
 
-    def __init__(self, coo: COOMatrix, *, length_policy: int = GBSP_LEN_3SMOOTH, u_tile: int = 0,
+    def __init__(self, coo: COOMatrix, *, length_policy: int = 0, u_tile: int = 0,
                  kahan_min_degree: int = 0, index_bytes: int = 0, max_channel_len: int = 0,
-                 rows_threads: int = 0, row_table_mode: int = 0, radix=None, stream=None,
+                 rows_threads: int = 0, row_table_mode: int = 0, radix=None, pass1_shape: int = 0,
+                 planner=None, options: Optional[GbspOptions] = None, stream=None,
                  csc: Optional[CompactCSC] = None):
         lib = load()
         self._lib = lib
         self._h = C.c_void_p()
         csc = csc if csc is not None else make_compact_csc(coo)
         self.rows, self.cols = coo.rows, coo.cols
-        o = GbspOptions(length_policy=length_policy, u_tile=u_tile, kahan_min_degree=kahan_min_degree,
-                        index_bytes=index_bytes, max_channel_len=max_channel_len,
-                        rows_threads=rows_threads, row_table_mode=row_table_mode)
-        for i, r in enumerate(radix or ()):
-            o.radix[i] = int(r)
+        o = make_options(options, radix=radix, planner=planner, length_policy=length_policy, u_tile=u_tile,
+                         kahan_min_degree=kahan_min_degree, index_bytes=index_bytes,
+                         max_channel_len=max_channel_len, rows_threads=rows_threads,
+                         row_table_mode=row_table_mode, pass1_shape=pass1_shape)
         cp = np.ascontiguousarray(csc.col_ptr, np.int32)
         ri = np.ascontiguousarray(csc.row_idx if coo.nnz else np.zeros(1, np.int32), np.int32)
         sc = np.ascontiguousarray(csc.sparse_cols if csc.n_sparse_cols else np.zeros(1, np.int32),
@@ -197,8 +227,9 @@ class Batch:
     graph_launch() replays it as a CUDA graph.  Each output equals what
     Plan(coo).execute() writes for the same matrix and options."""
 
-    def __init__(self, coos, *, length_policy: int = GBSP_LEN_3SMOOTH, kahan_min_degree: int = 0,
-                 index_bytes: int = 0, max_channel_len: int = 0, row_table_mode: int = 0, stream=None):
+    def __init__(self, coos, *, length_policy: int = 0, kahan_min_degree: int = 0,
+                 index_bytes: int = 0, max_channel_len: int = 0, row_table_mode: int = 0, pass1_shape: int = 0,
+                 planner=None, stream=None):
         lib = load()
         self._lib = lib
         self._h = C.c_void_p()
@@ -215,8 +246,9 @@ class Batch:
             sc = np.ascontiguousarray(csc.sparse_cols if csc.n_sparse_cols else np.zeros(1, np.int32), np.int32)
             keep += [cp, ri, sc]
             mats[i] = GbspMatrix(coo.rows, coo.cols, csc.n_sparse_cols, coo.nnz, _ip(cp), _ip(ri), _ip(sc))
-        o = GbspOptions(length_policy=length_policy, kahan_min_degree=kahan_min_degree, index_bytes=index_bytes,
-                        max_channel_len=max_channel_len, row_table_mode=row_table_mode)
+        o = make_options(None, planner=planner, length_policy=length_policy, kahan_min_degree=kahan_min_degree,
+                         index_bytes=index_bytes, max_channel_len=max_channel_len, row_table_mode=row_table_mode,
+                         pass1_shape=pass1_shape)
         check(lib.gbsp_batch_create(n, mats, C.byref(o), _stream_handle(stream), C.byref(self._h)),
               "gbsp_batch_create")
         self.infos = []

@@ -44,6 +44,23 @@ enum {
  *                      used by sparse_fft_csc_bluestein_cufft_smooth) */
 enum { GBSP_LEN_3SMOOTH = 3, GBSP_LEN_7SMOOTH = 7 };
 
+/* How a plan picks its radices, row block and pass-1 shape when the options
+ * leave them open.
+ *   GBSP_PLANNER_MODEL:   analytic cost model (default)
+ *   GBSP_PLANNER_LEARNED: the installed MLP cost model (gbsp_cost_model_set)
+ *                         scores every tuning candidate and the cheapest
+ *                         prediction is built.  The spectrum never depends
+ *                         on the choice. */
+enum { GBSP_PLANNER_MODEL = 0, GBSP_PLANNER_LEARNED = 1 };
+
+/* Pass-1 shapes (gbsp_options.pass1_shape, 1-based):
+ *   1: 256 rows x 32-column windows, full twiddle table
+ *   2: 256 x 32, half table      3: 128 x 64, full    4: 128 x 32, full
+ *   5: 128 x 64, half            6: 128 x 32, half */
+#define GBSP_N_PASS1_SHAPES 6
+/* Length of the cost-model feature vector (gbsp_plan_features). */
+#define GBSP_N_FEATURES 36
+
 typedef struct gbsp_plan_s* gbsp_plan_t;
 
 /* Tuning knobs.  Zero-initialise and set what you need; 0 means "default".
@@ -65,7 +82,9 @@ typedef struct {
     int radix[8];          /* channel FFT radix per stage, first to last, 0-terminated;
                               all zero = auto.  Allowed: 2 3 4 5 7 8 9 12 15 16 20 21
                               24 25 28 32 35 40; product = channel length                 */
-    int reserved[4];
+    int pass1_shape;       /* 0 = auto, else 1..GBSP_N_PASS1_SHAPES (must fit)          */
+    int planner;           /* GBSP_PLANNER_MODEL (0) or GBSP_PLANNER_LEARNED            */
+    int reserved[2];
 } gbsp_options;
 
 typedef struct {
@@ -84,6 +103,8 @@ typedef struct {
     int row_table_mode;    /* 0 full twiddle table in shared memory, 1 half table        */
     int rows_threads;      /* row-kernel block size in use                                */
     size_t device_bytes;   /* device memory held by the plan                              */
+    int pass1_shape;       /* pass-1 shape in use (1-based)                               */
+    int planner;           /* planner that chose the configuration                        */
 } gbsp_plan_info;
 
 int         gbsp_version(void);
@@ -218,6 +239,67 @@ int gbsp_batch_plan_info(gbsp_batch_t batch, int i, gbsp_plan_info* info);
 /* Reads and clears the device error flags of the batch and its sub-plans. */
 int gbsp_batch_error_flags(gbsp_batch_t batch, int* flags);
 int gbsp_batch_destroy(gbsp_batch_t batch);
+
+/* ---- tuning and the learned cost model ------------------------------------
+ * The reference fixes its configuration (--csc-tile, radix 9/3/2 order,
+ * src/sparse_fft_bluestein.cu:1996-2011); these entry points have no
+ * counterpart there.
+ *
+ * Candidates of a matrix: the `max_rows_cands` cheapest (radix sequence, row
+ * block) choices of the analytic model crossed with every pass-1 shape that
+ * fits.  out[i * n_p1 + j] pairs row choice i with shape j; each is `base`
+ * with radix, rows_threads and pass1_shape filled in.  Host-only (uses the
+ * current device's shared-memory limit, GB300's without a device). */
+int gbsp_plan_candidates(int rows, int cols, const gbsp_options* base, int max_rows_cands,
+                         gbsp_options* out, int cap, int* n_rows_cands, int* n_p1_cands);
+
+/* Cost-model features of (matrix, candidate): GBSP_N_FEATURES floats.
+ * [0,18) describe the matrix (log2 sizes, density, largest prime factors,
+ * fft_len, channels, column-degree histogram), [18,28) the row choice
+ * (block, stages, radices, shared memory, CTAs/SM, analytic cost) and
+ * [28,36) the pass-1 shape.  Host-only. */
+int gbsp_plan_features(int rows, int cols, int n_active, int nnz, const int* col_ptr,
+                       const gbsp_options* cand, float* out);
+
+/* One measured candidate: device time of pass 1 under its pass-1 shape and
+ * of the Bluestein rows under its radices and block (best of `reps`). */
+typedef struct {
+    gbsp_options opts;
+    float ms_pass1;
+    float ms_rows;
+} gbsp_tune_entry;
+
+/* Exhaustive autotuner: measures every candidate of the matrix on the
+ * current device (plans built, executed and destroyed in turn; one output
+ * buffer allocated for the duration).  Pass 1 depends only on the pass-1
+ * shape and the rows only on the row choice, so max(n_rows, n_p1) plans
+ * cover the whole cross product; entries[i * n_p1 + j] holds the composed
+ * times.  *best receives the candidate with the least total.  Blocking. */
+int gbsp_autotune(int rows, int cols, int n_active, int nnz, const int* col_ptr, const int* row_idx,
+                  const int* sparse_cols, const gbsp_options* base, int max_rows_cands, int reps,
+                  void* stream, gbsp_options* best, gbsp_tune_entry* entries, int cap,
+                  int* n_rows_cands, int* n_p1_cands);
+
+/* MLP cost model: n_in -> 64 -> 64 -> 1, ReLU, FP32.  Parameters, packed:
+ * W1[n_in][64], b1[64], W2[64][64], b2[64], w3[64], b3 (W[k][j] maps input
+ * k to unit j).  The kernels are deterministic (fixed reduction order). */
+#define GBSP_MLP_HIDDEN 64
+size_t gbsp_mlp_param_count(int n_in);
+/* y[i] = f(x[i]) for n rows of x (row-major n x n_in).  Device pointers. */
+int gbsp_mlp_forward(const float* d_params, int n_in, const float* d_x, int n, float* d_y, void* stream);
+/* Gradient of the loss mean_i (f(x_i) - t_i)^2 with respect to every
+ * parameter into d_grad (param_count floats) and the loss into *d_loss.
+ * d_work: scratch of gbsp_mlp_work_floats(n_in) floats. */
+size_t gbsp_mlp_work_floats(int n_in);
+int gbsp_mlp_backward(const float* d_params, int n_in, const float* d_x, const float* d_target, int n,
+                      float* d_grad, float* d_loss, float* d_work, void* stream);
+/* One Adam step (bias-corrected, step >= 1) on n_params parameters. */
+int gbsp_mlp_adam(float* d_params, const float* d_grad, float* d_m, float* d_v, size_t n_params, float lr,
+                  float beta1, float beta2, float eps, int step, void* stream);
+/* Installs the model GBSP_PLANNER_LEARNED uses (host arrays, copied):
+ * inputs are standardised as (x - feat_mean) / feat_scale before the
+ * network; the output is log(predicted ms).  n_in must be GBSP_N_FEATURES. */
+int gbsp_cost_model_set(const float* params, int n_in, const float* feat_mean, const float* feat_scale);
 
 #ifdef __cplusplus
 }
