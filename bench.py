@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=5,
+                    help="timed passes of the 64-matrix batched workload (0 skips it)")
     return ap.parse_args()
 
 
@@ -178,6 +180,59 @@ def fft_flops_per_row(info) -> float:
     import math
     L = info["fft_len"]
     return 2 * 5.0 * L * math.log2(L) + 6.0 * L + 6.0 * (info["n_active"] + info["cols"])
+
+
+def run_batched(args, torch, gb, synthetic) -> dict:
+    """64 matrices of uneven size and sparsity: the batched form (learned
+    plans, persistent work-queue launches, one CUDA graph per pass over the
+    batch) against the plain form (one plan per matrix, analytic planner,
+    its own launches).  Outputs (3.5 GB) exceed L2, so no flush is needed."""
+    from cuspfft_gb300 import costmodel
+    mats = synthetic.batch_matrices(64)
+    batch = gb.Batch(mats, length_policy=args.policy, planner="learned")
+    outs = batch.empty_outputs()
+    batch.set_outputs(outs)
+    plans = [gb.Plan(m, length_policy=args.policy) for m in mats]
+    pouts = [p.empty_output() for p in plans]
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.batch_steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.batch_steps
+
+    def plain():
+        for p, o in zip(plans, pouts):
+            p.execute(o)
+
+    ms_b = timed(batch.graph_launch)
+    ms_p = timed(plain)
+    flags = batch.error_flags()
+    meta = costmodel.load_model()["meta"] if costmodel.DEFAULT_MODEL.exists() else {}
+    n_sep = sum(1 for i in batch.infos if i["channels"] > 1)
+    res = {
+        "workload": "64 matrices, rows and cols log-uniform in [500, 12000] (half prime, half 2^a3^b5^c), "
+                    "density log-uniform in [1e-4, 1e-2], seed 4",
+        "unit": "matrices/s", "matrices_per_s": round(64e3 / ms_b, 1), "plain_matrices_per_s": round(64e3 / ms_p, 1),
+        "speedup_vs_plain": round(ms_p / ms_b, 3), "ms_per_batch": round(ms_b, 4), "plain_ms_per_batch": round(ms_p, 4),
+        "batched_form": "planner=learned, pass 1 in one work-queue launch, rows in one launch per size class, "
+                        "CUDA graph replay; cluster-split matrices through their own plans",
+        "plain_form": "64 plans (analytic planner), 2 launches each",
+        "cluster_matrices": n_sep, "error_flags": flags, "steps": args.batch_steps,
+        "output_bytes": int(sum(o.numel() * 8 for o in outs)),
+        "learned_regret_heldout": meta.get("regret_learned"), "analytic_regret_heldout": meta.get("regret_analytic"),
+    }
+    batch.close()
+    for p in plans:
+        p.close()
+    return res
 
 
 def main():
@@ -316,6 +371,10 @@ def main():
         st = fp64.check_stats(got, ref)
         acc = {"rel_l2_vs_fp64": st["rel_l2"], "max_abs": st["max_abs"], "rows_sampled": int(us.size)}
 
+    batched = None
+    if rank == 0 and args.batch_steps > 0:
+        batched = run_batched(args, torch, gb, synthetic)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(coo, args.cpu_budget)
@@ -336,6 +395,7 @@ def main():
             "output_gbs": round(out_bytes / (ms_per_step * 1e-3) / 1e9, 1),
             "gpu_launches": 2 * n_tiles * args.steps,
             "clocks": clk, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "accuracy": acc,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     plan.close()

@@ -385,17 +385,23 @@ __host__ __device__ constexpr bool radix_supported(int r) {
 constexpr int MAX_RADIX_NT1024 = 16;
 constexpr int MAX_RADIX_NT512 = 40;
 
+// Runs one stage of radix R; returns false (and touches nothing) when this
+// kernel was not compiled for R, so a plan/kernel mismatch is reported
+// instead of silently skipping the stage.
 template <int MODE, int MAXR, typename V>
-__device__ __forceinline__ void fft_stage_dispatch(int R, V* buf, int Lp, int m, uint32_t magic,
+__device__ __forceinline__ bool fft_stage_dispatch(int R, V* buf, int Lp, int m, uint32_t magic,
                                                    const V* tw, const V* filt, int tid, int nthreads) {
     switch (R) {
-#define GBSP_STAGE_CASE(r)                                                               \
-        case r:                                                                          \
-            if constexpr (r <= MAXR) fft_stage<r, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads); \
-            break;
+#define GBSP_STAGE_CASE(r)                                                                   \
+        case r:                                                                              \
+            if constexpr (r <= MAXR) {                                                       \
+                fft_stage<r, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads);              \
+                return true;                                                                 \
+            }                                                                                \
+            return false;
         GBSP_RADIX_LIST(GBSP_STAGE_CASE)
 #undef GBSP_STAGE_CASE
-        default: break;
+        default: return false;
     }
 }
 

@@ -519,13 +519,12 @@ struct RowsArgs {
 // forward network, filter, inverse network, Hermitian-paired output.  Whole
 // CTA (with the cluster when K > 1); ends on a barrier, so the next row may
 // overwrite buf at once.
-template <int MAXR>
+template <int MAXR, bool CLUSTER>
 __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& fd, int t, int q, float2* buf,
                                               const float2* twr, const float2* const* zsrc, uint64_t* bar,
-                                              uint32_t& parity, bool& timed_out) {
+                                              uint32_t& parity, int& err_bits) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int Lp = fd.Lp, K = a.K, cols = a.cols;
-    const bool CLUSTER = K > 1;
     const float2* preq = a.pre + (size_t)q * cols;
     const float2* filtq = a.filt + (size_t)q * Lp;
     const int half_slots = (int)(a.out_pitch >> 1);
@@ -537,43 +536,59 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     };
     const int u = a.u0 + t;
     const float2* srow = a.S + (size_t)t * a.s_pitch;
-    if (cols_even <= Lp) {
+    // (a single channel always has cols_even <= Lp: L >= 2*cols - 1)
+    if (!CLUSTER || cols_even <= Lp) {
         if (tid == 0) {
             fence_proxy_async_smem();
             mbar_expect_tx(bar, (uint32_t)cols_even * 8u);
             bulk_copy_g2s(buf, srow, (uint32_t)cols_even * 8u, bar);
         }
         for (int i = cols_even + tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
-        if (!mbar_wait_bounded(bar, parity)) timed_out = true;
+        if (!mbar_wait_bounded(bar, parity)) err_bits |= ERR_TIMEOUT;
         parity ^= 1u;
-        if (q != 0)  // channel pre-twiddle (channel 0's is 1)
+        if (CLUSTER && q != 0)  // channel pre-twiddle (channel 0's is 1)
             for (int c = tid; c < cols; c += nt) buf[c] = cmul(buf[c], __ldg(preq + c));
         __syncthreads();
-    } else {
-        for (int i = tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
-        __syncthreads();
-        // several input columns fold onto one slot: add section by section
-        for (int lo = 0; lo < cols; lo += Lp) {
-            const int hi = min(cols, lo + Lp);
-            for (int c = lo + tid; c < hi; c += nt)
-                buf[c - lo] = cadd(buf[c - lo], cmul(__ldcs(srow + c), __ldg(preq + c)));
-            __syncthreads();
+    } else if constexpr (CLUSTER) {
+        // Several input columns fold onto one slot: slot n gets
+        // sum_j pre[n + j*Lp] * x[n + j*Lp].  Each thread owns its slots, so
+        // no zero fill or barrier between sections; all of a slot's loads
+        // are issued before its products.
+        // L = K*Lp >= 2*cols - 1 gives cols/Lp <= K/2 + 1/(2Lp): at most
+        // K/2 + 1 sections
+        constexpr int MAXSEC = MAX_CHANNELS / 2 + 1;
+        for (int n = tid; n < Lp; n += nt) {
+            float2 xv[MAXSEC], pv[MAXSEC];
+#pragma unroll
+            for (int j = 0; j < MAXSEC; j++) {
+                const int c = n + j * Lp;
+                const bool ok = c < cols;
+                xv[j] = ok ? __ldcs(srow + c) : make_float2(0.f, 0.f);
+                pv[j] = ok ? __ldg(preq + c) : make_float2(0.f, 0.f);
+            }
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < MAXSEC; j++) acc = cadd(acc, cmul(xv[j], pv[j]));
+            buf[n] = acc;
         }
+        __syncthreads();
     }
     // forward DIF, filter multiply fused with the last stage, inverse DIT
     const int S1 = fd.nst - 1;
+    bool ok = true;
     for (int s = 0; s < S1; s++) {
-        fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s), (const float2*)nullptr,
-                                    tid, nt);
+        ok &= fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
+                                          (const float2*)nullptr, tid, nt);
         __syncthreads();
     }
-    fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
+    ok &= fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
     __syncthreads();
     for (int s = S1 - 1; s >= 0; s--) {
-        fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s), (const float2*)nullptr,
-                                    tid, nt);
+        ok &= fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
+                                          (const float2*)nullptr, tid, nt);
         __syncthreads();
     }
+    if (!ok) err_bits |= ERR_RADIX;
     if (CLUSTER) cg::this_cluster().sync();
 
     // Hermitian-paired row writer
@@ -581,37 +596,76 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     const bool two = (u2 != u);
     const int nslots = two ? 2 * half_slots : half_slots;
     const int lo = (int)((long)q * nslots / K), hi = (int)((long)(q + 1) * nslots / K);
-    for (int s = lo + tid; s < hi; s += nt) {
-        const int sel = s >= half_slots;
-        const int v = 2 * (s - sel * half_slots);
-        float2 o[2];
+    if (!CLUSTER) {
+        // Each thread takes WU slots per pass and issues all their loads (post
+        // chirp from L2, Z from shared memory) before any product, so the L2
+        // latency is paid once per WU slots.
+        constexpr int WU = 4;
+        for (int s0 = lo + tid; s0 < hi; s0 += WU * nt) {
+            int col[WU][2];
+            float2 pv[WU][2], zv[WU][2];
 #pragma unroll
-        for (int e = 0; e < 2; e++) {
-            const int vv = v + e;
-            float2 val = make_float2(0.f, 0.f);
-            if (vv <= hc) {
-                const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
-                if (CLUSTER) {
+            for (int w = 0; w < WU; w++) {
+                const int s = s0 + w * nt;
+                const int sel = s >= half_slots;
+                const int v = 2 * (s - sel * half_slots);
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int vv = v + e;
+                    const int c = (s >= hi || vv > hc) ? -1 : sel ? (vv == 0 ? 0 : cols - vv) : vv;
+                    col[w][e] = c;
+                    pv[w][e] = (c >= 0) ? __ldg(a.post + c) : make_float2(0.f, 0.f);
+                    zv[w][e] = buf[c < 0 ? 0 : c];
+                }
+            }
+#pragma unroll
+            for (int w = 0; w < WU; w++) {
+                const int s = s0 + w * nt;
+                if (s >= hi) break;
+                const int sel = s >= half_slots;
+                const int v = 2 * (s - sel * half_slots);
+                float2 o0 = col[w][0] < 0 ? make_float2(0.f, 0.f) : cmul(zv[w][0], pv[w][0]);
+                float2 o1 = col[w][1] < 0 ? make_float2(0.f, 0.f) : cmul(zv[w][1], pv[w][1]);
+                if (sel) {
+                    o0.y = -o0.y;
+                    o1.y = -o1.y;
+                }
+                const int row = sel ? u2 : u;
+                float4* dst = reinterpret_cast<float4*>(a.out + (size_t)row * a.out_pitch + v);
+                __stcs(dst, make_float4(o0.x, o0.y, o1.x, o1.y));
+            }
+        }
+    } else {
+        for (int s = lo + tid; s < hi; s += nt) {
+            const int sel = s >= half_slots;
+            const int v = 2 * (s - sel * half_slots);
+            float2 o[2];
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int vv = v + e;
+                float2 val = make_float2(0.f, 0.f);
+                if (vv <= hc) {
+                    const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
                     int n = c;
                     while (n >= Lp) n -= Lp;
                     for (int qq = 0; qq < K; qq++)
                         val = cadd(val, cmul(zsrc[qq][n], __ldg(a.post + (size_t)qq * cols + c)));
-                } else {
-                    val = cmul(buf[c], __ldg(a.post + c));
+                    if (sel) val.y = -val.y;
                 }
-                if (sel) val.y = -val.y;
+                o[e] = val;
             }
-            o[e] = val;
+            const int row = sel ? u2 : u;
+            float4* dst = reinterpret_cast<float4*>(a.out + (size_t)row * a.out_pitch + v);
+            __stcs(dst, make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
         }
-        const int row = sel ? u2 : u;
-        float4* dst = reinterpret_cast<float4*>(a.out + (size_t)row * a.out_pitch + v);
-        __stcs(dst, make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
     }
     if (CLUSTER) cg::this_cluster().sync();
     else __syncthreads();
 }
 
-template <int NTMAX>
+// CL: launched with a K-CTA cluster dimension (K > 1); single-channel plans
+// use the CL = false instance, which carries no cluster code.
+template <int NTMAX, bool CL>
 __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc fd, int* err) {
     extern __shared__ float4 smem_raw[];
     __shared__ uint64_t in_bar;
@@ -621,10 +675,10 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
     if (threadIdx.x == 0) mbar_init(&in_bar, 1);
 
     constexpr int MAXR = (NTMAX > 512) ? MAX_RADIX_NT1024 : MAX_RADIX_NT512;
-    const int K = a.K;  // K > 1 only in launches with a K-CTA cluster dimension
     int q = 0, cid = blockIdx.x, ncl = gridDim.x;
-    const float2* zsrc[MAX_CHANNELS];
-    if (K > 1) {
+    const float2* zsrc[CL ? MAX_CHANNELS : 1];
+    if constexpr (CL) {
+        const int K = a.K;
         cg::cluster_group cl = cg::this_cluster();
         q = (int)cl.block_rank();
         cid = blockIdx.x / K;
@@ -636,12 +690,12 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
         zsrc[0] = buf;
     }
     uint32_t parity = 0;
-    bool timed_out = false;
+    int err_bits = 0;
     __syncthreads();
     for (int t = cid; t < a.tile_rows; t += ncl)
-        bluestein_row<MAXR>(a, fd, t, q, buf, twr, zsrc, &in_bar, parity, timed_out);
-    if (timed_out) {
-        atomicOr(err, ERR_TIMEOUT);
+        bluestein_row<MAXR, CL>(a, fd, t, q, buf, twr, zsrc, &in_bar, parity, err_bits);
+    if (err_bits) atomicOr(err, err_bits);
+    if (err_bits & ERR_TIMEOUT) {
         // a copy that never signalled may still be in flight: wait once more
         // (bounded) before the shared memory is released
         mbar_wait_bounded(&in_bar, parity ^ 1u);
@@ -678,7 +732,7 @@ k_bluestein_rows_batch(const RowsBatch* __restrict__ descs, const long* __restri
     }
     const float2* zsrc[1] = {buf};
     uint32_t parity = 0;
-    bool timed_out = false;
+    int err_bits = 0;
     int loaded = -1;
     const long total = row_begin[nmat];
     __syncthreads();
@@ -703,13 +757,11 @@ k_bluestein_rows_batch(const RowsBatch* __restrict__ descs, const long* __restri
             __syncthreads();
             loaded = m;
         }
-        bluestein_row<MAXR>(cur.a, cur.fd, (int)(t - row_begin[m]), 0, buf, twr, zsrc, &in_bar, parity,
-                            timed_out);
+        bluestein_row<MAXR, false>(cur.a, cur.fd, (int)(t - row_begin[m]), 0, buf, twr, zsrc, &in_bar, parity,
+                            err_bits);
     }
-    if (timed_out) {
-        atomicOr(err, ERR_TIMEOUT);
-        mbar_wait_bounded(&in_bar, parity ^ 1u);
-    }
+    if (err_bits) atomicOr(err, err_bits);
+    if (err_bits & ERR_TIMEOUT) mbar_wait_bounded(&in_bar, parity ^ 1u);
 }
 
 }  // namespace gbsp

@@ -27,6 +27,7 @@ GBSP_HD constexpr size_t p1_head_bytes(int ku, int cw) {
 }
 constexpr long long WAIT_LIMIT = 1LL << 26;  // bounded spin on an mbarrier (~seconds)
 constexpr int ERR_TIMEOUT = 1;              // bit set in the plan's error word
+constexpr int ERR_RADIX = 2;                // a stage radix the kernel was not compiled for
 
 struct FFTDesc {
     int Lp;                     // channel FFT length

@@ -207,7 +207,7 @@ cudaLaunchConfig_t rows_config(const gbsp_plan_s* p, unsigned grid, unsigned nt,
 // clusters (K > 1) of p->rows_threads threads can be resident at once.
 template <bool CL, int NTMAX>
 int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
-    auto kern = gbsp::k_bluestein_rows<NTMAX>;
+    auto kern = gbsp::k_bluestein_rows<NTMAX, CL>;
     if (int rc = allow_full_smem(kern)) return rc;
     *cap = 0;
     if (!CL) {
@@ -245,7 +245,7 @@ template <bool CL, int NTMAX>
 int rows_launch_t(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch, cudaStream_t st) {
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>,
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, CL>,
                                rows_args(p, p->d_S, p->s_pitch, u0, n, d_out, out_pitch), p->fd, p->d_err));
     return GBSP_OK;
 }
@@ -683,7 +683,7 @@ int rows_launch_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int 
                      size_t out_pitch, cudaStream_t st) {
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX>,
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, CL>,
                                rows_args(p, S, s_pitch, u0, n, d_out, out_pitch), p->fd, p->d_err));
     return GBSP_OK;
 }

@@ -197,8 +197,9 @@ int gbsp_column_sums(gbsp_plan_t plan, int u0, int n_rows, void* d_s, size_t s_p
 int gbsp_execute_noalloc(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream);
 
 /* Reads and clears the plan's device error flags (synchronises the device).
- * Bit 0: a bounded wait inside a kernel gave up (the result of that
- * transform is not valid).  0 means no error was recorded. */
+ * Bit 0: a bounded wait inside a kernel gave up; bit 1: a stage radix the
+ * row kernel was not compiled for (plan/kernel mismatch).  Either way the
+ * result of that transform is not valid.  0 means no error was recorded. */
 int gbsp_plan_error_flags(gbsp_plan_t plan, int* flags);
 
 /* ---- batches ---------------------------------------------------------------
