@@ -15,6 +15,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstring>
 #include <cstdlib>
 #include <functional>
 #include <stdexcept>
@@ -68,9 +69,15 @@ void print_check(const char* method, const gbsp_cli::HostSpectrum& ref, const Sp
     if (ref.rows == 0) return;
     const int fc = ref.freq_cols;
     std::vector<float> h((size_t)ref.rows * fc * 2);
-    cudaError_t e = cudaMemcpy2D(h.data(), (size_t)fc * 8, r.d_output, (size_t)r.output_cols * 8,
-                                 (size_t)fc * 8, ref.rows, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e));
+    if (!r.h_output.empty()) {  // streamed methods return the spectrum on the host
+        for (int row = 0; row < ref.rows; row++)
+            std::memcpy(h.data() + (size_t)row * fc * 2, r.h_output.data() + (size_t)row * r.output_cols,
+                        (size_t)fc * 8);
+    } else {
+        cudaError_t e = cudaMemcpy2D(h.data(), (size_t)fc * 8, r.d_output, (size_t)r.output_cols * 8,
+                                     (size_t)fc * 8, ref.rows, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e));
+    }
     double max_abs = 0, max_rel = 0, sum_sq = 0;
     const size_t n = (size_t)ref.rows * fc;
     for (size_t i = 0; i < n; i++) {
@@ -95,13 +102,14 @@ void usage(const char* prog) {
             "  --csc-mixed-radix  Binary CSC + Bluestein, fft_len next 3-smooth (sm_103a kernels)\n"
             "  --csc-mixed-radix-graph  Same, replayed as one CUDA graph\n"
             "  --csc-cufft-smooth  Binary CSC + Bluestein, fft_len next 7-smooth (own kernels, no cuFFT)\n"
+            "  --csc-stockham-stream  Streaming variant: tiles copied to pinned host memory (3-smooth)\n"
+            "  --csc-stockham-cufft-stream  Streaming variant, 7-smooth length (own kernels, no cuFFT)\n"
             "  --csc-tile N     Bluestein rows per tile (default: 1024)\n"
             "  --cpu-reference  Host FP64 reference spectrum; every method is checked against it\n"
             "  --repeat N       1 warm-up + N timed runs; report median, min, max (default 1)\n"
             "  (--csc-bluestein --csc-stockham --csc-stockham-smem --csc-stockham-cufft\n"
-            "   --csc-stockham-stream --csc-stockham-cufft-stream --csc-stockham-graph --spfft\n"
-            "   --csc-binary-lut --csc-binary-stockham-smem are accepted and report\n"
-            "   'not in this build')\n",
+            "   --csc-stockham-graph --spfft --csc-binary-lut --csc-binary-stockham-smem are\n"
+            "   accepted and report 'not in this build')\n",
             prog);
 }
 
@@ -113,7 +121,7 @@ int main(int argc, char** argv) {
     if (first == "--help" || first == "-h") { usage(argv[0]); return 0; }
 
     bool run_dense = true, run_sparse = true;
-    bool mixed = false, mixed_graph = false, smooth = false, cpu_ref = false;
+    bool mixed = false, mixed_graph = false, smooth = false, cpu_ref = false, stream3 = false, stream7 = false;
     std::vector<std::string> unbuilt;
     int tile = 1024, repeat = 1;
     try {
@@ -125,14 +133,15 @@ int main(int argc, char** argv) {
             else if (f == "--csc-mixed-radix-graph") mixed_graph = true;
             else if (f == "--csc-cufft-smooth") smooth = true;
             else if (f == "--cpu-reference") cpu_ref = true;
+            else if (f == "--csc-stockham-stream") stream3 = true;
+            else if (f == "--csc-stockham-cufft-stream") stream7 = true;
             else if (f == "--csc-tile" || f == "--repeat") {
                 if (++i >= argc) throw std::runtime_error(f + " requires an integer value");
                 int v = std::stoi(argv[i]);
                 if (v <= 0) throw std::runtime_error(f + " must be positive");
                 (f == "--csc-tile" ? tile : repeat) = v;
             } else if (f == "--csc-bluestein" || f == "--csc-stockham" || f == "--csc-stockham-smem" ||
-                       f == "--csc-stockham-cufft" || f == "--csc-stockham-stream" ||
-                       f == "--csc-stockham-cufft-stream" || f == "--csc-stockham-graph" ||
+                       f == "--csc-stockham-cufft" || f == "--csc-stockham-graph" ||
                        f == "--spfft" || f == "--csc-binary-lut" || f == "--csc-binary-stockham-smem") {
                 unbuilt.push_back(f);
             } else {
@@ -175,6 +184,10 @@ int main(int argc, char** argv) {
              [&] { return sparse_fft_csc_bluestein_cufft_smooth(coo, tile); }},
             {mixed_graph, "Sparse CSC (mr-graph)", "Sparse CSC mr-graph",
              [&] { return sparse_fft_csc_bluestein_mixed_radix_graph(coo, tile); }},
+            {stream3, "Sparse CSC (Stockham stream)", "Sparse CSC Stockham stream",
+             [&] { return sparse_fft_csc_stockham_streaming(coo, tile, 0); }},
+            {stream7, "Sparse CSC (cufft stream)", "Sparse CSC cufft stream",
+             [&] { return sparse_fft_csc_bluestein_cufft_streaming(coo, tile); }},
         };
         for (auto& m : methods) {
             if (!run_sparse || !m.on) continue;

@@ -513,6 +513,10 @@ struct RowsArgs {
     float2* out;
     size_t out_pitch;
     int K, rows, cols, u0, tile_rows;
+    // output row r goes to out row r - map_lo when r < map_split, else to
+    // r - map_hi (identity: map_split = INT_MAX, map_lo = 0); lets a tile of
+    // rows u and rows-u land in a small slab for streaming to the host
+    int map_split, map_lo, map_hi;
 };
 
 // One Bluestein row t of the tile (u = u0 + t), channel q of K: input,
@@ -631,7 +635,8 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                     o1.y = -o1.y;
                 }
                 const int row = sel ? u2 : u;
-                float4* dst = reinterpret_cast<float4*>(a.out + (size_t)row * a.out_pitch + v);
+                const int drow = row < a.map_split ? row - a.map_lo : row - a.map_hi;
+                float4* dst = reinterpret_cast<float4*>(a.out + (size_t)drow * a.out_pitch + v);
                 __stcs(dst, make_float4(o0.x, o0.y, o1.x, o1.y));
             }
         }
@@ -655,7 +660,8 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                 o[e] = val;
             }
             const int row = sel ? u2 : u;
-            float4* dst = reinterpret_cast<float4*>(a.out + (size_t)row * a.out_pitch + v);
+            const int drow = row < a.map_split ? row - a.map_lo : row - a.map_hi;
+            float4* dst = reinterpret_cast<float4*>(a.out + (size_t)drow * a.out_pitch + v);
             __stcs(dst, make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
         }
     }

@@ -6,6 +6,7 @@
 // Bluestein rows: k_twiddle_sum (pass 1) and k_bluestein_rows (convolution +
 // R2C writer).
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -223,7 +224,7 @@ int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
 }
 
 gbsp::RowsArgs rows_args(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
-                         size_t out_pitch) {
+                         size_t out_pitch, int map_split = INT_MAX, int map_lo = 0, int map_hi = 0) {
     gbsp::RowsArgs a;
     a.S = S;
     a.s_pitch = s_pitch;
@@ -238,6 +239,9 @@ gbsp::RowsArgs rows_args(const gbsp_plan_s* p, const float2* S, size_t s_pitch, 
     a.cols = p->cols;
     a.u0 = u0;
     a.tile_rows = n;
+    a.map_split = map_split;
+    a.map_lo = map_lo;
+    a.map_hi = map_hi;
     return a;
 }
 
@@ -688,6 +692,22 @@ int rows_launch_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int 
     return GBSP_OK;
 }
 
+// the row kernel with fully specified arguments (input tile, output slab
+// and row map)
+template <bool CL, int NTMAX>
+int rows_launch_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, CL>, a, p->fd, p->d_err));
+    return GBSP_OK;
+}
+
+int launch_rows_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
+    if (p->K == 1)
+        return p->rows_ntmax == 512 ? rows_launch_args<false, 512>(p, a, st) : rows_launch_args<false, 1024>(p, a, st);
+    return p->rows_ntmax == 512 ? rows_launch_args<true, 512>(p, a, st) : rows_launch_args<true, 1024>(p, a, st);
+}
+
 int launch_rows_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
                      size_t out_pitch, cudaStream_t st) {
     if (p->K == 1)
@@ -1089,3 +1109,85 @@ int gbsp_batch_destroy(gbsp_batch_t b) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Streaming to host memory: tiles of Bluestein rows are computed into one of
+// two small device slabs (output rows u and rows-u of the tile, remapped by
+// the row writer) while the previous slab is copied to the host on a second
+// stream.  Device memory beyond the plan: two slabs of 2 x tile x pitch.
+// ===========================================================================
+namespace {
+
+struct StreamRes {
+    cudaStream_t cs = nullptr;
+    cudaEvent_t done[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    void* slab[2] = {nullptr, nullptr};
+    ~StreamRes() {
+        for (int b = 0; b < 2; b++) {
+            if (done[b]) cudaEventDestroy(done[b]);
+            if (copied[b]) cudaEventDestroy(copied[b]);
+            if (slab[b]) cudaFree(slab[b]);
+        }
+        if (cs) cudaStreamDestroy(cs);
+    }
+};
+
+}  // namespace
+
+extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch, int tile_rows, void* stream) {
+    if (!p || !h_out) return set_error(GBSP_ERR_INVALID, "gbsp_execute_to_host: null argument");
+    if (out_pitch < (size_t)p->out_cols || (out_pitch & 1))
+        return set_error(GBSP_ERR_INVALID, "gbsp_execute_to_host: out_pitch must be even and >= cols/2+1");
+    if (tile_rows < 0) return set_error(GBSP_ERR_INVALID, "gbsp_execute_to_host: tile_rows must be >= 0");
+    const int tile = std::min(tile_rows > 0 ? tile_rows : 1024, p->u_tile);
+    cudaStream_t st = (cudaStream_t)stream;
+    StreamRes r;
+    const size_t slab_bytes = (size_t)2 * tile * out_pitch * sizeof(float2);
+    GB_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; b++) {
+        GB_CUDA(cudaEventCreateWithFlags(&r.done[b], cudaEventDisableTiming));
+        GB_CUDA(cudaEventCreateWithFlags(&r.copied[b], cudaEventDisableTiming));
+        cudaError_t e = cudaMalloc(&r.slab[b], slab_bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            r.slab[b] = nullptr;
+            return set_error(GBSP_ERR_ALLOC, std::string("gbsp_execute_to_host: slab: ") + cudaGetErrorString(e));
+        }
+    }
+    const size_t row_bytes = out_pitch * sizeof(float2);
+    char* host = static_cast<char*>(h_out);
+    int rc = GBSP_OK;
+    int t = 0;
+    for (int u0 = 0; u0 < p->half_rows && rc == GBSP_OK; u0 += tile, t++) {
+        const int n = std::min(tile, p->half_rows - u0);
+        const int b = t & 1;
+        if (t >= 2) GB_CUDA(cudaStreamWaitEvent(st, r.copied[b], 0));
+        // rows u in [u0, u0+n) -> slab rows [0, n); their mirrors rows - u
+        // (u >= 1, rows - u != u) form [hi_first, rows - u0] -> slab rows n..
+        const int u_last = u0 + n - 1;
+        int hi_first = p->rows - u_last;
+        if (2 * u_last == p->rows) hi_first++;  // the middle row is its own mirror
+        const int hi_last = p->rows - std::max(u0, 1);
+        const int n_hi = std::max(0, hi_last - hi_first + 1);
+        if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p->d_post, st))) break;
+        const gbsp::RowsArgs a =
+            rows_args(p, p->d_S, p->s_pitch, u0, n, r.slab[b], out_pitch, u0 + n, u0, hi_first - n);
+        if ((rc = launch_rows_args(p, a, st))) break;
+        GB_CUDA(cudaEventRecord(r.done[b], st));
+        GB_CUDA(cudaStreamWaitEvent(r.cs, r.done[b], 0));
+        GB_CUDA(cudaMemcpy2DAsync(host + (size_t)u0 * row_bytes, row_bytes, r.slab[b], row_bytes, row_bytes, n,
+                                  cudaMemcpyDeviceToHost, r.cs));
+        if (n_hi > 0)
+            GB_CUDA(cudaMemcpy2DAsync(host + (size_t)hi_first * row_bytes, row_bytes,
+                                      static_cast<char*>(r.slab[b]) + (size_t)n * row_bytes, row_bytes, row_bytes,
+                                      n_hi, cudaMemcpyDeviceToHost, r.cs));
+        GB_CUDA(cudaEventRecord(r.copied[b], r.cs));
+    }
+    cudaError_t e1 = cudaStreamSynchronize(r.cs);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    if (rc) return rc;
+    if (e1 != cudaSuccess || e2 != cudaSuccess)
+        return set_error(GBSP_ERR_CUDA, std::string("gbsp_execute_to_host: ") +
+                                            cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    return GBSP_OK;
+}

@@ -6,6 +6,8 @@
 // written against the reference (try / catch / cudaGetLastError) behave the
 // same way.  Every device buffer is owned by an RAII holder, so a throw
 // leaks nothing (the reference leaks on throw).
+#include <algorithm>
+
 #include <cuda_runtime.h>
 
 #include <stdexcept>
@@ -149,6 +151,42 @@ SparseFFTResult run_graph(const COOMatrix& coo, int u_tile, int policy) {
     return r;
 }
 
+struct PinnedBuf {
+    void* p = nullptr;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+// Streaming form: the spectrum goes tile by tile into pinned host memory and
+// is returned in h_output with d_output = nullptr, as the reference's
+// streaming methods do (src/sparse_fft_bluestein.cu:1276-1296).
+SparseFFTResult run_streaming(const COOMatrix& coo, int u_tile, int policy) {
+    MemDelta mem;
+    PlanHolder ph;
+    gbsp_plan_info info;
+    make_plan(coo, u_tile, policy, ph, info);
+    const size_t n = (size_t)coo.rows * info.output_pitch;
+    PinnedBuf host;
+    cuda_check(cudaMallocHost(&host.p, std::max<size_t>(n, 1) * sizeof(cuFloatComplex)), "cudaMallocHost");
+    cuda_check(cudaDeviceSynchronize(), "setup");
+    Events ev;
+    cuda_check(cudaEventRecord(ev.a, nullptr), "cudaEventRecord");
+    check(gbsp_execute_to_host(ph.p, host.p, (size_t)info.output_pitch, u_tile, nullptr), "gbsp_execute_to_host");
+    cuda_check(cudaEventRecord(ev.b, nullptr), "cudaEventRecord");
+    cuda_check(cudaEventSynchronize(ev.b), "cudaEventSynchronize");
+    float ms = 0.f;
+    cuda_check(cudaEventElapsedTime(&ms, ev.a, ev.b), "cudaEventElapsedTime");
+    SparseFFTResult r;
+    r.mem_bytes = mem.finish();
+    r.output_cols = info.output_pitch;
+    r.ms = ms;
+    r.d_output = nullptr;
+    const cuFloatComplex* h = static_cast<const cuFloatComplex*>(host.p);
+    r.h_output.assign(h, h + n);
+    return r;
+}
+
 [[noreturn]] void not_built(const char* name) {
     throw std::runtime_error(std::string(name) + ": not in this build");
 }
@@ -219,11 +257,14 @@ SparseFFTResult sparse_fft_csc_bluestein_smem(const COOMatrix&, int) {
 SparseFFTResult sparse_fft_csc_bluestein_cufft(const COOMatrix&, int) {
     not_built("sparse_fft_csc_bluestein_cufft");
 }
-SparseFFTResult sparse_fft_csc_stockham_streaming(const COOMatrix&, int, int) {
-    not_built("sparse_fft_csc_stockham_streaming");
+// Streaming methods: same transform as the two hot methods, output to host.
+// fft_backend only selects the FFT library in the reference; here every
+// backend runs the sm_103a kernels (3-smooth length).
+SparseFFTResult sparse_fft_csc_stockham_streaming(const COOMatrix& coo, int u_tile, int) {
+    return run_streaming(coo, u_tile, GBSP_LEN_3SMOOTH);
 }
-SparseFFTResult sparse_fft_csc_bluestein_cufft_streaming(const COOMatrix&, int) {
-    not_built("sparse_fft_csc_bluestein_cufft_streaming");
+SparseFFTResult sparse_fft_csc_bluestein_cufft_streaming(const COOMatrix& coo, int u_tile) {
+    return run_streaming(coo, u_tile, GBSP_LEN_7SMOOTH);
 }
 SparseFFTResult sparse_fft_csc_stockham_graph(const COOMatrix&, int) {
     not_built("sparse_fft_csc_stockham_graph");

@@ -182,6 +182,17 @@ class Plan:
         check(self._lib.gbsp_execute(self._h, C.c_void_p(out.data_ptr()), out.shape[1],
                                      _stream_handle(stream)), "gbsp_execute")
 
+    def execute_to_host(self, host_out, tile_rows: int = 0, stream=None) -> None:
+        """Streams the spectrum into host_out (rows x pitch complex64, CPU,
+        contiguous; pinned memory lets the copies overlap the compute) one
+        tile of Bluestein rows at a time.  Blocks until done."""
+        if str(host_out.dtype) != "torch.complex64" or host_out.is_cuda or not host_out.is_contiguous():
+            raise ValueError("host_out must be a contiguous complex64 CPU tensor")
+        if host_out.dim() != 2 or host_out.shape[0] < self.rows:
+            raise ValueError("host_out must have shape (rows, pitch)")
+        check(self._lib.gbsp_execute_to_host(self._h, C.c_void_p(host_out.data_ptr()), host_out.shape[1],
+                                             tile_rows, _stream_handle(stream)), "gbsp_execute_to_host")
+
     def execute_profiled(self, out, stream=None) -> tuple[float, float]:
         """Runs execute() with events around each phase; returns (ms pass 1, ms rows)."""
         a, b = C.c_float(), C.c_float()

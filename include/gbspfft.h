@@ -196,6 +196,18 @@ int gbsp_column_sums(gbsp_plan_t plan, int u0, int n_rows, void* d_s, size_t s_p
  * Asynchronous on `stream`, like gbsp_execute. */
 int gbsp_execute_noalloc(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream);
 
+/* Streams the transform to host memory: the reference's streaming methods
+ * (sparse_fft_csc_stockham_streaming / _cufft_streaming,
+ * src/sparse_fft_bluestein.cu:912-1145, 1150-1296), for outputs larger than
+ * device memory.  Tiles of tile_rows Bluestein rows (0 = 1024, at most the
+ * plan's u_tile) are computed into one of two device slabs holding the
+ * tile's output rows u and rows-u while the other slab is copied to h_out on
+ * a second stream.  h_out: rows * out_pitch complex64 (pinned memory lets
+ * the copies overlap); columns [cols/2+1, out_pitch) are written as zeros.
+ * Extra device memory: 2 slabs of 2 * tile * out_pitch complex64.  Blocks
+ * until the whole spectrum is in h_out. */
+int gbsp_execute_to_host(gbsp_plan_t plan, void* h_out, size_t out_pitch, int tile_rows, void* stream);
+
 /* Reads and clears the plan's device error flags (synchronises the device).
  * Bit 0: a bounded wait inside a kernel gave up; bit 1: a stage radix the
  * row kernel was not compiled for (plan/kernel mismatch).  Either way the
