@@ -184,7 +184,7 @@ int main(int argc, char** argv) {
              [&] { return sparse_fft_csc_bluestein_cufft_smooth(coo, tile); }},
             {mixed_graph, "Sparse CSC (mr-graph)", "Sparse CSC mr-graph",
              [&] { return sparse_fft_csc_bluestein_mixed_radix_graph(coo, tile); }},
-            {stream3, "Sparse CSC (Stockham stream)", "Sparse CSC Stockham stream",
+            {stream3, "Sparse CSC (Stockham strm)", "Sparse CSC Stockham strm",
              [&] { return sparse_fft_csc_stockham_streaming(coo, tile, 0); }},
             {stream7, "Sparse CSC (cufft stream)", "Sparse CSC cufft stream",
              [&] { return sparse_fft_csc_bluestein_cufft_streaming(coo, tile); }},

@@ -91,7 +91,7 @@ def test_cli_streaming_methods(cuda, tmp_path):
                           "--csc-stockham-cufft-stream", "--csc-tile", "40"], capture_output=True, text=True,
                          timeout=300)
     assert res.returncode == 0, res.stderr
-    assert "Sparse CSC (cufft stream)" in res.stdout and "Sparse CSC (Stockham stream)" in res.stdout
+    assert "Sparse CSC (cufft stream)" in res.stdout and "Sparse CSC (Stockham strm)" in res.stdout
     checks = [ln for ln in res.stdout.splitlines() if ln.strip().startswith("check")]
     assert len(checks) == 2, res.stdout
     for ln in checks:
