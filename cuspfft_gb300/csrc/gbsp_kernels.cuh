@@ -120,11 +120,15 @@ __global__ void k_table_filter_input(double2* __restrict__ bq, int cols, int L, 
 }
 
 // One forward DIF stage (any radix R <= MAX_RADIX) over K channels in global
-// memory, FP64: the R-point DFT by its definition and the stage twiddles,
-// every root evaluated from an exactly reduced integer phase.  Used once per
-// plan for the filter spectrum, so it follows the row kernel's network.
+// memory, FP64, out of place: one thread per output element, which sums its
+// butterfly's R inputs against the R-point roots by definition and applies
+// the stage twiddle, every root evaluated from an exactly reduced integer
+// phase.  Used once per plan for the filter spectrum, so it follows the row
+// kernel's network.  (One thread per element keeps every SM busy: FP64 runs
+// at a small fraction of the FP32 rate on this part.)
 constexpr int MAX_RADIX = 64;
-__global__ void k_dif_stage_f64(double2* __restrict__ data, int K, int Lp, int R, int m) {
+__global__ void k_dif_stage_f64(const double2* __restrict__ src, double2* __restrict__ dst, int K, int Lp, int R,
+                                int m) {
     __shared__ double2 root[MAX_RADIX];  // W_R^e, e < R
     if (R > MAX_RADIX) return;
     for (int e = threadIdx.x; e < R; e += blockDim.x) {
@@ -133,25 +137,20 @@ __global__ void k_dif_stage_f64(double2* __restrict__ data, int K, int Lp, int R
         root[e] = make_double2(cs, sn);
     }
     __syncthreads();
-    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    int nb = Lp / R;
-    if (idx >= (long)K * nb) return;
-    int ch = (int)(idx / nb);
-    int t = (int)(idx - (long)ch * nb);
-    double2* x = data + (size_t)ch * Lp;
-    int j = t / m, k = t - (t / m) * m;
-    int base = j * R * m + k;
-    long long l = Lp / (R * m);
-    double2 in[MAX_RADIX];
-    for (int s = 0; s < R; s++) in[s] = x[base + s * m];
-    for (int q = 0; q < R; q++) {
-        double2 acc = make_double2(0.0, 0.0);
-        for (int s = 0, e = 0; s < R; s++, e = (e + q) % R) acc = cadd(acc, cmul(in[s], root[e]));
-        long long e = ((long long)q * k * l) % Lp;
-        double sn, cs;
-        sincospi(-2.0 * (double)e / (double)Lp, &sn, &cs);
-        x[base + q * m] = cmul(acc, make_double2(cs, sn));
-    }
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)K * Lp) return;
+    const int ch = (int)(idx / Lp);
+    const int pos = (int)(idx - (long)ch * Lp);  // = j*R*m + q*m + k
+    const int span = R * m;
+    const int j = pos / span, rem = pos - j * span, q = rem / m, k = rem - q * m;
+    const double2* x = src + (size_t)ch * Lp + (size_t)j * span + k;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int s = 0, e = 0; s < R; s++, e = (e + q) % R) acc = cadd(acc, cmul(x[(size_t)s * m], root[e]));
+    const long long l = Lp / span;
+    const long long ph = ((long long)q * k * l) % Lp;
+    double sn, cs;
+    sincospi(-2.0 * (double)ph / (double)Lp, &sn, &cs);
+    dst[idx] = cmul(acc, make_double2(cs, sn));
 }
 
 // filt[ch][q*(Lp/R) + t] = (float)(spec[ch][t*R + q] * scale): the filter in the

@@ -57,6 +57,8 @@ struct gbsp_plan_s {
     size_t rows_smem = 0;
     size_t device_bytes = 0;
     std::vector<void*> allocs;
+    char* arena = nullptr;           // one allocation carved into the plan's buffers
+    size_t arena_size = 0, arena_off = 0;
 };
 
 namespace {
@@ -69,8 +71,16 @@ namespace {
                              std::string(#call) + ": " + cudaGetErrorString(e_));        \
     } while (0)
 
+// Carves `bytes` (256-byte aligned) from the plan's arena when it has room,
+// else allocates on its own.
 int dev_alloc(gbsp_plan_s* p, void** ptr, size_t bytes) {
     bytes = std::max<size_t>(bytes, 16);
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    if (p->arena && p->arena_off + need <= p->arena_size) {
+        *ptr = p->arena + p->arena_off;
+        p->arena_off += need;
+        return GBSP_OK;
+    }
     cudaError_t e = cudaMalloc(ptr, bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -82,17 +92,50 @@ int dev_alloc(gbsp_plan_s* p, void** ptr, size_t bytes) {
     return GBSP_OK;
 }
 
+// Per-device limits the planner needs, queried once per device (a full
+// cudaGetDeviceProperties costs far more than the two attributes).
+struct DeviceLimits {
+    size_t smem_optin = 0;
+    int sms = 0;
+};
+int device_limits(int dev, DeviceLimits* out) {
+    constexpr int kMaxDev = 64;
+    static std::mutex mu;
+    static DeviceLimits cache[kMaxDev];
+    if (dev < 0 || dev >= kMaxDev) return set_error(GBSP_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (cache[dev].sms == 0) {
+        int optin = 0, sms = 0;
+        GB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cache[dev].smem_optin = (size_t)optin;
+        cache[dev].sms = sms;
+    }
+    *out = cache[dev];
+    return GBSP_OK;
+}
+
 // Lets `kern` take all the opt-in shared memory of a CTA.  The limit is a
 // property of the kernel, shared by every plan in the process; one fixed
-// value keeps a later, smaller plan from invalidating an earlier one.
+// value keeps a later, smaller plan from invalidating an earlier one.  Done
+// once per (kernel, device).
+std::mutex g_smem_mu;
+std::vector<std::pair<const void*, int>> g_smem_done;  // (kernel, device) already raised
+
 template <typename F>
 int allow_full_smem(F* kern) {
-    cudaFuncAttributes fa;
-    int dev = 0, optin = 0;
-    GB_CUDA(cudaFuncGetAttributes(&fa, kern));
+    int dev = 0;
     GB_CUDA(cudaGetDevice(&dev));
-    GB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    const std::pair<const void*, int> key((const void*)kern, dev);
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    if (std::find(g_smem_done.begin(), g_smem_done.end(), key) != g_smem_done.end()) return GBSP_OK;
+    cudaFuncAttributes fa;
+    DeviceLimits lim;
+    GB_CUDA(cudaFuncGetAttributes(&fa, kern));
+    if (int rc = device_limits(dev, &lim)) return rc;
+    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)lim.smem_optin - (int)fa.sharedSizeBytes));
+    g_smem_done.push_back(key);
     return GBSP_OK;
 }
 
@@ -335,10 +378,10 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     gbsp_options o = o_in ? *o_in : gbsp_options{};
     if (force_p1) o.pass1_shape = force_p1;
     GB_CUDA(cudaGetDevice(&p->device));
-    cudaDeviceProp prop;
-    GB_CUDA(cudaGetDeviceProperties(&prop, p->device));
-    const size_t smem_cap = prop.sharedMemPerBlockOptin;
-    const int sms = prop.multiProcessorCount;
+    DeviceLimits lim;
+    if (int rc0 = device_limits(p->device, &lim)) return rc0;
+    const size_t smem_cap = lim.smem_optin;
+    const int sms = lim.sms;
     const int tmode = o.row_table_mode;
     if (tmode < 0 || tmode > 2) return set_error(GBSP_ERR_INVALID, "row_table_mode must be 0, 1 or 2");
     if (o.pass1_shape < 0 || o.pass1_shape > gbsp::N_P1_SHAPES)
@@ -435,6 +478,32 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
             task_col[(size_t)w * VM + i] = (uint8_t)ts[i].col;
         }
     }
+    // one device allocation for every buffer of the plan
+    {
+        const int ntw_all = std::max(fft_tw_count(p->fd), 1);
+        const size_t s_pitch_all = ((size_t)p->s_cols + 15) & ~(size_t)15;
+        const size_t sizes[] = {slot0.size(), task.size() * sizeof(int2), task_col.size(),
+                                (size_t)std::max(p->nnz, 1) * p->idx_bytes, sizeof(int),
+                                (size_t)p->ntab * sizeof(float2), (size_t)p->K * p->cols * sizeof(float2),
+                                (size_t)p->K * p->cols * sizeof(float2), (size_t)p->K * p->Lp * sizeof(float2),
+                                (size_t)ntw_all * sizeof(float2), (size_t)p->K * p->Lp * sizeof(double2),
+                                (size_t)p->K * p->Lp * sizeof(double2),
+                                (size_t)p->u_tile * s_pitch_all * sizeof(float2)};
+        size_t total = 0;
+        for (size_t b : sizes) total += (std::max<size_t>(b, 16) + 255) & ~(size_t)255;
+        void* base = nullptr;
+        cudaError_t e = cudaMalloc(&base, total);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(GBSP_ERR_ALLOC, std::string("cudaMalloc(") + std::to_string(total) +
+                                                 "): " + cudaGetErrorString(e));
+        }
+        p->allocs.push_back(base);
+        p->device_bytes += total;
+        p->arena = static_cast<char*>(base);
+        p->arena_size = total;
+        p->arena_off = 0;
+    }
     if ((rc = dev_alloc(p, (void**)&p->d_win_slot0, slot0.size()))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_win_task, task.size() * sizeof(int2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_win_task_col, task_col.size()))) return rc;
@@ -479,22 +548,25 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
                                                                p->fd.twoff[s]);
         GB_CUDA(cudaGetLastError());
     }
-    double2* d_spec = nullptr;
-    GB_CUDA(cudaMalloc((void**)&d_spec, (size_t)K * Lp * sizeof(double2)));
-    gbsp::k_table_filter_input<<<blocks_for((long)K * Lp, 256), 256, 0, st>>>(d_spec, cols, p->L, K, Lp);
+    // FP64 filter workspace, kept with the plan (freeing it here would
+    // synchronise the whole device)
+    double2* d_spec[2] = {nullptr, nullptr};  // ping-pong: the stages run out of place
+    if ((rc = dev_alloc(p, (void**)&d_spec[0], (size_t)K * Lp * sizeof(double2)))) return rc;
+    if ((rc = dev_alloc(p, (void**)&d_spec[1], (size_t)K * Lp * sizeof(double2)))) return rc;
+    gbsp::k_table_filter_input<<<blocks_for((long)K * Lp, 256), 256, 0, st>>>(d_spec[0], cols, p->L, K, Lp);
     cudaError_t e = cudaGetLastError();
-    for (int s = 0; s < p->fd.nst && e == cudaSuccess; s++) {
-        const long nbf = (long)K * (Lp / p->fd.R[s]);
-        gbsp::k_dif_stage_f64<<<blocks_for(nbf, 128), 128, 0, st>>>(d_spec, K, Lp, p->fd.R[s], p->fd.m[s]);
+    int cur = 0;
+    for (int s = 0; s < p->fd.nst && e == cudaSuccess; s++, cur ^= 1) {
+        gbsp::k_dif_stage_f64<<<blocks_for((long)K * Lp, 128), 128, 0, st>>>(d_spec[cur], d_spec[cur ^ 1], K, Lp,
+                                                                             p->fd.R[s], p->fd.m[s]);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
         gbsp::k_table_filter_final<<<blocks_for((long)K * Lp, 256), 256, 0, st>>>(
-            p->d_filt, d_spec, K, Lp, p->fd.R[p->fd.nst - 1], 1.0 / (double)p->L);
+            p->d_filt, d_spec[cur], K, Lp, p->fd.R[p->fd.nst - 1], 1.0 / (double)p->L);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(d_spec);
     if (e != cudaSuccess)
         return set_error(GBSP_ERR_CUDA, std::string("plan tables: ") + cudaGetErrorString(e));
 
@@ -874,13 +946,13 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
     if (!b) return set_error(GBSP_ERR_ALLOC, "gbsp_batch_create: out of host memory");
     b->count = count;
     int rc = GBSP_OK;
-    cudaDeviceProp prop;
-    if (cudaGetDevice(&b->device) != cudaSuccess || cudaGetDeviceProperties(&prop, b->device) != cudaSuccess) {
+    DeviceLimits lim;
+    if (cudaGetDevice(&b->device) != cudaSuccess || device_limits(b->device, &lim) != GBSP_OK) {
         free_batch(b);
         return set_error(GBSP_ERR_CUDA, "gbsp_batch_create: no CUDA device");
     }
-    const size_t smem_cap = prop.sharedMemPerBlockOptin;
-    const int sms = prop.multiProcessorCount;
+    const size_t smem_cap = lim.smem_optin;
+    const int sms = lim.sms;
     // one pass-1 shape for the batch: the largest row count decides it
     int max_rows = 1;
     bool u32 = false;
