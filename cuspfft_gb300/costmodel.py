@@ -109,7 +109,7 @@ def dataset_matrices(n: int, seed: int):
         yield synthetic.uniform_matrix(r, c, max(1, int(round(r * c * d))), seed * 100003 + i)
 
 
-def collect(mats, policy: int = GBSP_LEN_7SMOOTH, reps: int = 3, log_every: int = 100) -> dict:
+def collect(mats, policy: int = GBSP_LEN_7SMOOTH, reps: int = 3, log_every: int = 100, **opts) -> dict:
     N = len(mats)
     ds = {
         "M": np.zeros((N, N_M), np.float32), "R": np.zeros((N, MAX_R, N_R), np.float32),
@@ -122,7 +122,7 @@ def collect(mats, policy: int = GBSP_LEN_7SMOOTH, reps: int = 3, log_every: int 
     t0 = time.time()
     for k, coo in enumerate(mats):
         csc = make_compact_csc(coo)
-        tr = tuning.autotune(coo, csc=csc, reps=reps, length_policy=policy)
+        tr = tuning.autotune(coo, csc=csc, reps=reps, length_policy=policy, **opts)
         ds["n_rows"][k], ds["n_p1"][k] = tr.n_rows, tr.n_p1
         ds["dims"][k] = (coo.rows, coo.cols, coo.nnz)
         ds["ms_rows"][k, :tr.n_rows] = tr.ms_rows
@@ -275,6 +275,7 @@ def main(argv=None) -> None:
     t.add_argument("--out", default=str(DEFAULT_MODEL))
     t.add_argument("--epochs", type=int, default=300)
     t.add_argument("--seed", type=int, default=0)
+    t.add_argument("--large", action="store_true", help="also evaluate on the 40421 x 40421 matrix")
     a = ap.parse_args(argv)
     if a.cmd == "collect":
         mats = list(dataset_matrices(a.train + a.test, a.seed))
@@ -291,8 +292,26 @@ def main(argv=None) -> None:
         pred = predict(model, Xt)
         meta = {"train_matrices": int(tr.size), "test_matrices": int(te.size), "epochs": a.epochs,
                 "regret_learned": regret(ds, te, pred), "regret_analytic": regret(ds, te)}
+        if a.large:
+            meta["large_matrix"] = evaluate_large(model)
         save_model(a.out, model, meta)
         print(json.dumps(meta))
+
+
+def evaluate_large(model: dict) -> dict:
+    """The 40421 x 40421 power-law adjacency (~351k nnz, 4-byte indices):
+    exhaustive tuning against the learned and the analytic choice."""
+    coo = synthetic.config_matrix("uniform_powerlaw_40421")
+    ds = collect([coo], reps=2, log_every=0, index_bytes=4)
+    X, _, _ = compose(ds, [0])
+    pred = predict(model, X)
+    nr, npp = int(ds["n_rows"][0]), int(ds["n_p1"][0])
+    t = ds["ms_rows"][0, :nr, None].astype(np.float64) + ds["ms_pass1"][0, None, :npp]
+    return {"shape": [coo.rows, coo.cols], "nnz": coo.nnz, "index_bytes": 4, "candidates": nr * npp,
+            "best_ms": float(t.min()), "learned_ms": float(t.ravel()[int(np.argmin(pred))]),
+            "analytic_ms": float(t[0, 0]),
+            "regret_learned": float(t.ravel()[int(np.argmin(pred))] / t.min() - 1.0),
+            "regret_analytic": float(t[0, 0] / t.min() - 1.0)}
 
 
 if __name__ == "__main__":
