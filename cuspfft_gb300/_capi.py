@@ -53,7 +53,8 @@ class GbspOptions(C.Structure):
         ("radix", C.c_int * 8),
         ("pass1_shape", C.c_int),
         ("planner", C.c_int),
-        ("reserved", C.c_int * 2),
+        ("channel_mode", C.c_int),
+        ("reserved", C.c_int * 1),
     ]
 
     def radices(self) -> tuple:
@@ -67,7 +68,7 @@ class GbspPlanInfo(C.Structure):
         ("n_stages", C.c_int), ("radix", C.c_int * 16), ("output_cols", C.c_int),
         ("output_pitch", C.c_int), ("half_rows", C.c_int), ("u_tile", C.c_int),
         ("index_bytes", C.c_int), ("row_table_mode", C.c_int), ("rows_threads", C.c_int),
-        ("device_bytes", C.c_size_t), ("pass1_shape", C.c_int), ("planner", C.c_int),
+        ("device_bytes", C.c_size_t), ("pass1_shape", C.c_int), ("planner", C.c_int), ("channel_mode", C.c_int),
     ]
 
     def as_dict(self) -> dict:

@@ -516,20 +516,31 @@ struct RowsArgs {
     // r - map_hi (identity: map_split = INT_MAX, map_lo = 0); lets a tile of
     // rows u and rows-u land in a small slab for streaming to the host
     int map_split, map_lo, map_hi;
+    // ROW_SEQ: per-CTA scratch for the first K-1 channels of a row,
+    // (K-1) x Lp complex per CTA, CTA b at zscratch + b*(K-1)*Lp
+    float2* zscratch;
 };
+
+// How the K channels of a long row are laid out on the GPU.
+//   ROW_SINGLE  K == 1, one CTA per row
+//   ROW_CLUSTER one CTA per channel, the K CTAs of a row one thread-block
+//               cluster; the output combine reads the peers' buffers (DSMEM)
+//   ROW_SEQ     one CTA runs the K channels one after another; the first K-1
+//               results wait in an L2-resident scratch for the combine
+constexpr int ROW_SINGLE = 0, ROW_CLUSTER = 1, ROW_SEQ = 2;
 
 // One Bluestein row t of the tile (u = u0 + t), channel q of K: input,
 // forward network, filter, inverse network, Hermitian-paired output.  Whole
 // CTA (with the cluster when K > 1); ends on a barrier, so the next row may
 // overwrite buf at once.
-template <int MAXR, bool CLUSTER>
+template <int MAXR, int MODE>
 __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& fd, int t, int q, float2* buf,
                                               const float2* twr, const float2* const* zsrc, uint64_t* bar,
                                               uint32_t& parity, int& err_bits) {
+    constexpr bool CLUSTER = MODE == ROW_CLUSTER;
+    constexpr bool MULTI = MODE != ROW_SINGLE;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int Lp = fd.Lp, K = a.K, cols = a.cols;
-    const float2* preq = a.pre + (size_t)q * cols;
-    const float2* filtq = a.filt + (size_t)q * Lp;
     const int half_slots = (int)(a.out_pitch >> 1);
     const int hc = cols / 2;
     const int cols_even = (cols + 1) & ~1;
@@ -539,58 +550,69 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     };
     const int u = a.u0 + t;
     const float2* srow = a.S + (size_t)t * a.s_pitch;
-    // (a single channel always has cols_even <= Lp: L >= 2*cols - 1)
-    if (!CLUSTER || cols_even <= Lp) {
-        if (tid == 0) {
-            fence_proxy_async_smem();
-            mbar_expect_tx(bar, (uint32_t)cols_even * 8u);
-            bulk_copy_g2s(buf, srow, (uint32_t)cols_even * 8u, bar);
-        }
-        for (int i = cols_even + tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
-        if (!mbar_wait_bounded(bar, parity)) err_bits |= ERR_TIMEOUT;
-        parity ^= 1u;
-        if (CLUSTER && q != 0)  // channel pre-twiddle (channel 0's is 1)
-            for (int c = tid; c < cols; c += nt) buf[c] = cmul(buf[c], __ldg(preq + c));
-        __syncthreads();
-    } else if constexpr (CLUSTER) {
-        // Several input columns fold onto one slot: slot n gets
-        // sum_j pre[n + j*Lp] * x[n + j*Lp].  Each thread owns its slots, so
-        // no zero fill or barrier between sections; all of a slot's loads
-        // are issued before its products.
-        // L = K*Lp >= 2*cols - 1 gives cols/Lp <= K/2 + 1/(2Lp): at most
-        // K/2 + 1 sections
-        constexpr int MAXSEC = MAX_CHANNELS / 2 + 1;
-        for (int n = tid; n < Lp; n += nt) {
-            float2 xv[MAXSEC], pv[MAXSEC];
-#pragma unroll
-            for (int j = 0; j < MAXSEC; j++) {
-                const int c = n + j * Lp;
-                const bool ok = c < cols;
-                xv[j] = ok ? __ldcs(srow + c) : make_float2(0.f, 0.f);
-                pv[j] = ok ? __ldg(preq + c) : make_float2(0.f, 0.f);
-            }
-            float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int j = 0; j < MAXSEC; j++) acc = cadd(acc, cmul(xv[j], pv[j]));
-            buf[n] = acc;
-        }
-        __syncthreads();
-    }
-    // forward DIF, filter multiply fused with the last stage, inverse DIT
-    const int S1 = fd.nst - 1;
     bool ok = true;
-    for (int s = 0; s < S1; s++) {
-        ok &= fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                          (const float2*)nullptr, tid, nt);
+    // ROW_SEQ runs every channel of the row here; the other modes one
+    const int q_end = (MODE == ROW_SEQ) ? K : q + 1;
+    for (int qc = (MODE == ROW_SEQ) ? 0 : q; qc < q_end; qc++) {
+        const float2* preq = a.pre + (size_t)qc * cols;
+        const float2* filtq = a.filt + (size_t)qc * Lp;
+        // (a single channel always has cols_even <= Lp: L >= 2*cols - 1)
+        if (!MULTI || cols_even <= Lp) {
+            if (tid == 0) {
+                fence_proxy_async_smem();
+                mbar_expect_tx(bar, (uint32_t)cols_even * 8u);
+                bulk_copy_g2s(buf, srow, (uint32_t)cols_even * 8u, bar);
+            }
+            for (int i = cols_even + tid; i < Lp; i += nt) buf[i] = make_float2(0.f, 0.f);
+            if (!mbar_wait_bounded(bar, parity)) err_bits |= ERR_TIMEOUT;
+            parity ^= 1u;
+            if (MULTI && qc != 0)  // channel pre-twiddle (channel 0's is 1)
+                for (int c = tid; c < cols; c += nt) buf[c] = cmul(buf[c], __ldg(preq + c));
+            __syncthreads();
+        } else if constexpr (MULTI) {
+            // Several input columns fold onto one slot: slot n gets
+            // sum_j pre[n + j*Lp] * x[n + j*Lp].  Each thread owns its slots, so
+            // no zero fill or barrier between sections; all of a slot's loads
+            // are issued before its products.
+            // L = K*Lp >= 2*cols - 1 gives cols/Lp <= K/2 + 1/(2Lp): at most
+            // K/2 + 1 sections
+            constexpr int MAXSEC = MAX_CHANNELS / 2 + 1;
+            for (int n = tid; n < Lp; n += nt) {
+                float2 xv[MAXSEC], pv[MAXSEC];
+#pragma unroll
+                for (int j = 0; j < MAXSEC; j++) {
+                    const int c = n + j * Lp;
+                    const bool ok = c < cols;
+                    xv[j] = ok ? __ldcs(srow + c) : make_float2(0.f, 0.f);
+                    pv[j] = ok ? __ldg(preq + c) : make_float2(0.f, 0.f);
+                }
+                float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < MAXSEC; j++) acc = cadd(acc, cmul(xv[j], pv[j]));
+                buf[n] = acc;
+            }
+            __syncthreads();
+        }
+        // forward DIF, filter multiply fused with the last stage, inverse DIT
+        const int S1 = fd.nst - 1;
+        for (int s = 0; s < S1; s++) {
+            ok &= fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
+                                              (const float2*)nullptr, tid, nt);
+            __syncthreads();
+        }
+        ok &= fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
         __syncthreads();
-    }
-    ok &= fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
-    __syncthreads();
-    for (int s = S1 - 1; s >= 0; s--) {
-        ok &= fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                          (const float2*)nullptr, tid, nt);
-        __syncthreads();
-    }
+        for (int s = S1 - 1; s >= 0; s--) {
+            ok &= fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
+                                              (const float2*)nullptr, tid, nt);
+            __syncthreads();
+        }
+        if (MODE == ROW_SEQ && qc < K - 1) {  // park the channel for the combine
+            float2* dst = a.zscratch + ((size_t)blockIdx.x * (K - 1) + qc) * Lp;
+            for (int i = tid; i < Lp; i += nt) dst[i] = buf[i];
+            __syncthreads();
+        }
+    }  // channels
     if (!ok) err_bits |= ERR_RADIX;
     if (CLUSTER) cg::this_cluster().sync();
 
@@ -598,8 +620,10 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     const int u2 = (u == 0) ? 0 : a.rows - u;
     const bool two = (u2 != u);
     const int nslots = two ? 2 * half_slots : half_slots;
-    const int lo = (int)((long)q * nslots / K), hi = (int)((long)(q + 1) * nslots / K);
-    if (!CLUSTER) {
+    // a cluster splits the row's output slots among its CTAs
+    const int qw = CLUSTER ? q : 0, kw = CLUSTER ? K : 1;
+    const int lo = (int)((long)qw * nslots / kw), hi = (int)((long)(qw + 1) * nslots / kw);
+    if (!MULTI) {
         // Each thread takes WU slots per pass and issues all their loads (post
         // chirp from L2, Z from shared memory) before any product, so the L2
         // latency is paid once per WU slots.
@@ -668,9 +692,10 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     else __syncthreads();
 }
 
-// CL: launched with a K-CTA cluster dimension (K > 1); single-channel plans
-// use the CL = false instance, which carries no cluster code.
-template <int NTMAX, bool CL>
+// MODE: ROW_SINGLE, ROW_CLUSTER (launched with a K-CTA cluster dimension)
+// or ROW_SEQ; single-channel plans use the ROW_SINGLE instance, which
+// carries no multi-channel code.
+template <int NTMAX, int MODE>
 __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc fd, int* err) {
     extern __shared__ float4 smem_raw[];
     __shared__ uint64_t in_bar;
@@ -681,8 +706,8 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
 
     constexpr int MAXR = (NTMAX > 512) ? MAX_RADIX_NT1024 : MAX_RADIX_NT512;
     int q = 0, cid = blockIdx.x, ncl = gridDim.x;
-    const float2* zsrc[CL ? MAX_CHANNELS : 1];
-    if constexpr (CL) {
+    const float2* zsrc[MODE == ROW_SINGLE ? 1 : MAX_CHANNELS];
+    if constexpr (MODE == ROW_CLUSTER) {
         const int K = a.K;
         cg::cluster_group cl = cg::this_cluster();
         q = (int)cl.block_rank();
@@ -691,6 +716,11 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
 #pragma unroll
         for (int i = 0; i < MAX_CHANNELS; i++)
             zsrc[i] = (i < K) ? cl.map_shared_rank(buf, i) : buf;
+    } else if constexpr (MODE == ROW_SEQ) {
+        const int K = a.K;
+#pragma unroll
+        for (int i = 0; i < MAX_CHANNELS; i++)
+            zsrc[i] = (i < K - 1) ? a.zscratch + ((size_t)blockIdx.x * (K - 1) + i) * fd.Lp : buf;
     } else {
         zsrc[0] = buf;
     }
@@ -698,7 +728,7 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
     int err_bits = 0;
     __syncthreads();
     for (int t = cid; t < a.tile_rows; t += ncl)
-        bluestein_row<MAXR, CL>(a, fd, t, q, buf, twr, zsrc, &in_bar, parity, err_bits);
+        bluestein_row<MAXR, MODE>(a, fd, t, q, buf, twr, zsrc, &in_bar, parity, err_bits);
     if (err_bits) atomicOr(err, err_bits);
     if (err_bits & ERR_TIMEOUT) {
         // a copy that never signalled may still be in flight: wait once more
@@ -762,7 +792,7 @@ k_bluestein_rows_batch(const RowsBatch* __restrict__ descs, const long* __restri
             __syncthreads();
             loaded = m;
         }
-        bluestein_row<MAXR, false>(cur.a, cur.fd, (int)(t - row_begin[m]), 0, buf, twr, zsrc, &in_bar, parity,
+        bluestein_row<MAXR, ROW_SINGLE>(cur.a, cur.fd, (int)(t - row_begin[m]), 0, buf, twr, zsrc, &in_bar, parity,
                             err_bits);
     }
     if (err_bits) atomicOr(err, err_bits);

@@ -54,6 +54,8 @@ struct gbsp_plan_s {
     int p1_grid = 0;
     size_t p1_smem = 0;
     int rows_grid = 0, rows_threads = 1024, rows_ntmax = 1024;
+    int row_mode = 0;                // gbsp::ROW_SINGLE / ROW_CLUSTER / ROW_SEQ
+    float2* d_zscratch = nullptr;    // ROW_SEQ: rows_grid x (K-1) x Lp channel results
     size_t rows_smem = 0;
     size_t device_bytes = 0;
     std::vector<void*> allocs;
@@ -228,9 +230,10 @@ int launch_pass1(const gbsp_plan_s* p, int u0, int n, float2* S, size_t sp, cons
 // cluster of K CTAs per row otherwise.  NTMAX is the compiled block-size
 // bound (1024: 64 registers a thread; 512: 128, for radices above 16); the
 // block itself has p->rows_threads threads.
-template <bool CL>
+template <int MODE>
 cudaLaunchConfig_t rows_config(const gbsp_plan_s* p, unsigned grid, unsigned nt, cudaStream_t st,
                                cudaLaunchAttribute* attr) {
+    constexpr bool CL = MODE == gbsp::ROW_CLUSTER;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(nt);
@@ -247,11 +250,13 @@ cudaLaunchConfig_t rows_config(const gbsp_plan_s* p, unsigned grid, unsigned nt,
     return cfg;
 }
 
-// Sets the kernel's shared-memory limit and returns how many CTAs (K == 1) or
-// clusters (K > 1) of p->rows_threads threads can be resident at once.
-template <bool CL, int NTMAX>
+// Sets the kernel's shared-memory limit and returns how many CTAs (single
+// channel, sequential channels) or clusters of p->rows_threads threads can be
+// resident at once.
+template <int MODE, int NTMAX>
 int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
-    auto kern = gbsp::k_bluestein_rows<NTMAX, CL>;
+    constexpr bool CL = MODE == gbsp::ROW_CLUSTER;
+    auto kern = gbsp::k_bluestein_rows<NTMAX, MODE>;
     if (int rc = allow_full_smem(kern)) return rc;
     *cap = 0;
     if (!CL) {
@@ -260,7 +265,7 @@ int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
         *cap = nb * sms;
     } else {
         cudaLaunchAttribute attr[1];
-        cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)(p->K * sms), p->rows_threads, nullptr, attr);
+        cudaLaunchConfig_t cfg = rows_config<MODE>(p, (unsigned)(p->K * sms), p->rows_threads, nullptr, attr);
         GB_CUDA(cudaOccupancyMaxActiveClusters(cap, kern, &cfg));
     }
     return GBSP_OK;
@@ -285,25 +290,37 @@ gbsp::RowsArgs rows_args(const gbsp_plan_s* p, const float2* S, size_t s_pitch, 
     a.map_split = map_split;
     a.map_lo = map_lo;
     a.map_hi = map_hi;
+    a.zscratch = p->d_zscratch;
     return a;
 }
 
-template <bool CL, int NTMAX>
-int rows_launch_t(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch, cudaStream_t st) {
+// the row kernel with fully specified arguments (input tile, output slab
+// and row map)
+template <int MODE, int NTMAX>
+int rows_launch_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
     cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, CL>,
-                               rows_args(p, p->d_S, p->s_pitch, u0, n, d_out, out_pitch), p->fd, p->d_err));
+    cudaLaunchConfig_t cfg = rows_config<MODE>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
+    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, MODE>, a, p->fd, p->d_err));
     return GBSP_OK;
 }
 
-int launch_rows(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch,
-                cudaStream_t st) {
-    if (p->K == 1)
-        return p->rows_ntmax == 512 ? rows_launch_t<false, 512>(p, u0, n, d_out, out_pitch, st)
-                                    : rows_launch_t<false, 1024>(p, u0, n, d_out, out_pitch, st);
-    return p->rows_ntmax == 512 ? rows_launch_t<true, 512>(p, u0, n, d_out, out_pitch, st)
-                                : rows_launch_t<true, 1024>(p, u0, n, d_out, out_pitch, st);
+// Instances: single channel and clusters with both block-size bounds,
+// sequential channels with the 512-thread bound.
+int launch_rows_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
+    using namespace gbsp;
+    const bool n512 = p->rows_ntmax == 512;
+    switch (p->row_mode) {
+        case ROW_SINGLE:
+            return n512 ? rows_launch_args<ROW_SINGLE, 512>(p, a, st) : rows_launch_args<ROW_SINGLE, 1024>(p, a, st);
+        case ROW_CLUSTER:
+            return n512 ? rows_launch_args<ROW_CLUSTER, 512>(p, a, st) : rows_launch_args<ROW_CLUSTER, 1024>(p, a, st);
+        default:
+            return rows_launch_args<ROW_SEQ, 512>(p, a, st);
+    }
+}
+
+int launch_rows(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch, cudaStream_t st) {
+    return launch_rows_args(p, rows_args(p, p->d_S, p->s_pitch, u0, n, d_out, out_pitch), st);
 }
 
 // Block size and radices are already chosen; pick the compiled variant and
@@ -315,15 +332,24 @@ int rows_prepare(gbsp_plan_s* p, int sms) {
     if (p->rows_threads > p->rows_ntmax || p->rows_threads < 32 || p->rows_threads % 32)
         return set_error(GBSP_ERR_INVALID, "rows_threads must be a multiple of 32, at most 512 when a "
                                            "radix exceeds 16, at most 1024 otherwise");
+    using namespace gbsp;
+    if (p->K == 1) p->row_mode = ROW_SINGLE;
+    else if (p->row_mode != ROW_SEQ || p->rows_ntmax != 512) p->row_mode = ROW_CLUSTER;
     int cap = 0, rc;
-    const bool cl = p->K > 1;
-    if (p->rows_ntmax == 512)
-        rc = cl ? rows_capacity<true, 512>(p, sms, &cap) : rows_capacity<false, 512>(p, sms, &cap);
-    else
-        rc = cl ? rows_capacity<true, 1024>(p, sms, &cap) : rows_capacity<false, 1024>(p, sms, &cap);
+    const bool n512 = p->rows_ntmax == 512;
+    switch (p->row_mode) {
+        case ROW_SINGLE:
+            rc = n512 ? rows_capacity<ROW_SINGLE, 512>(p, sms, &cap) : rows_capacity<ROW_SINGLE, 1024>(p, sms, &cap);
+            break;
+        case ROW_CLUSTER:
+            rc = n512 ? rows_capacity<ROW_CLUSTER, 512>(p, sms, &cap) : rows_capacity<ROW_CLUSTER, 1024>(p, sms, &cap);
+            break;
+        default:
+            rc = rows_capacity<ROW_SEQ, 512>(p, sms, &cap);
+    }
     if (rc) return rc;
     if (cap < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row kernel does not fit on an SM");
-    p->rows_grid = cap * p->K;
+    p->rows_grid = (p->row_mode == ROW_CLUSTER) ? cap * p->K : cap;
     return GBSP_OK;
 }
 
@@ -400,6 +426,12 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->Lp = sp.Lp;
     p->fd = sp.ranked[0].fd;
     p->rows_threads = sp.ranked[0].nt;
+    if (o.channel_mode < 0 || o.channel_mode > 2)
+        return set_error(GBSP_ERR_INVALID, "channel_mode must be 0 (auto), 1 (clusters) or 2 (sequential)");
+    // multi-channel rows run sequentially in one CTA unless clusters are asked
+    // for (measured on GB300: 1-4 % faster at 2 channels, 10-12 % at 4-5);
+    // settled in rows_prepare
+    p->row_mode = (o.channel_mode == 1) ? gbsp::ROW_CLUSTER : gbsp::ROW_SEQ;
 
     p->half_rows = p->rows / 2 + 1;
     p->out_cols = p->cols / 2 + 1;
@@ -488,7 +520,10 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
                                 (size_t)p->K * p->cols * sizeof(float2), (size_t)p->K * p->Lp * sizeof(float2),
                                 (size_t)ntw_all * sizeof(float2), (size_t)p->K * p->Lp * sizeof(double2),
                                 (size_t)p->K * p->Lp * sizeof(double2),
-                                (size_t)p->u_tile * s_pitch_all * sizeof(float2)};
+                                (size_t)p->u_tile * s_pitch_all * sizeof(float2),
+                                (p->row_mode == gbsp::ROW_SEQ)
+                                    ? (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2)
+                                    : 0};
         size_t total = 0;
         for (size_t b : sizes) total += (std::max<size_t>(b, 16) + 255) & ~(size_t)255;
         void* base = nullptr;
@@ -505,6 +540,9 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         p->arena_off = 0;
     }
     if ((rc = dev_alloc(p, (void**)&p->d_win_slot0, slot0.size()))) return rc;
+    if (p->row_mode == gbsp::ROW_SEQ &&
+        (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2))))
+        return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_win_task, task.size() * sizeof(int2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_win_task_col, task_col.size()))) return rc;
     if ((rc = dev_alloc(p, &p->d_row_idx, (size_t)std::max(p->nnz, 1) * p->idx_bytes))) return rc;
@@ -634,6 +672,7 @@ int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
     info->device_bytes = p->device_bytes;
     info->pass1_shape = p->p1_shape;
     info->planner = p->planner;
+    info->channel_mode = p->K == 1 ? 0 : (p->row_mode == gbsp::ROW_SEQ ? 2 : 1);
     return GBSP_OK;
 }
 
@@ -754,39 +793,9 @@ int noalloc_scratch_address(int device, void** addr) {
 }
 
 // the row kernel reading its input rows from an explicit S tile
-template <bool CL, int NTMAX>
-int rows_launch_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
-                     size_t out_pitch, cudaStream_t st) {
-    cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, CL>,
-                               rows_args(p, S, s_pitch, u0, n, d_out, out_pitch), p->fd, p->d_err));
-    return GBSP_OK;
-}
-
-// the row kernel with fully specified arguments (input tile, output slab
-// and row map)
-template <bool CL, int NTMAX>
-int rows_launch_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
-    cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = rows_config<CL>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, CL>, a, p->fd, p->d_err));
-    return GBSP_OK;
-}
-
-int launch_rows_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
-    if (p->K == 1)
-        return p->rows_ntmax == 512 ? rows_launch_args<false, 512>(p, a, st) : rows_launch_args<false, 1024>(p, a, st);
-    return p->rows_ntmax == 512 ? rows_launch_args<true, 512>(p, a, st) : rows_launch_args<true, 1024>(p, a, st);
-}
-
 int launch_rows_from(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
                      size_t out_pitch, cudaStream_t st) {
-    if (p->K == 1)
-        return p->rows_ntmax == 512 ? rows_launch_from<false, 512>(p, S, s_pitch, u0, n, d_out, out_pitch, st)
-                                    : rows_launch_from<false, 1024>(p, S, s_pitch, u0, n, d_out, out_pitch, st);
-    return p->rows_ntmax == 512 ? rows_launch_from<true, 512>(p, S, s_pitch, u0, n, d_out, out_pitch, st)
-                                : rows_launch_from<true, 1024>(p, S, s_pitch, u0, n, d_out, out_pitch, st);
+    return launch_rows_args(p, rows_args(p, S, s_pitch, u0, n, d_out, out_pitch), st);
 }
 
 }  // namespace

@@ -84,7 +84,11 @@ typedef struct {
                               24 25 28 32 35 40; product = channel length                 */
     int pass1_shape;       /* 0 = auto, else 1..GBSP_N_PASS1_SHAPES (must fit)          */
     int planner;           /* GBSP_PLANNER_MODEL (0) or GBSP_PLANNER_LEARNED            */
-    int reserved[2];
+    int channel_mode;      /* convolutions split into channels: 1 = one CTA per channel
+                              in a thread-block cluster, 2 = one CTA runs the channels in
+                              turn (results parked in an L2-resident scratch); 0 = auto
+                              (2 with 512-thread row blocks, else 1)                      */
+    int reserved[1];
 } gbsp_options;
 
 typedef struct {
@@ -105,6 +109,7 @@ typedef struct {
     size_t device_bytes;   /* device memory held by the plan                              */
     int pass1_shape;       /* pass-1 shape in use (1-based)                               */
     int planner;           /* planner that chose the configuration                        */
+    int channel_mode;      /* 0 single channel, 1 clusters, 2 sequential channels         */
 } gbsp_plan_info;
 
 int         gbsp_version(void);

@@ -59,14 +59,27 @@ def test_random_shapes(cuda, rows, cols, policy):
     (gb.GBSP_LEN_3SMOOTH, 250, 3), (gb.GBSP_LEN_7SMOOTH, 250, 3), (gb.GBSP_LEN_7SMOOTH, 340, 2),
     (gb.GBSP_LEN_7SMOOTH, 170, 4), (gb.GBSP_LEN_7SMOOTH, 120, 6), (gb.GBSP_LEN_7SMOOTH, 100, 7),
     (gb.GBSP_LEN_7SMOOTH, 84, 8)])
-def test_channel_split_clusters(cuda, policy, max_len, channels):
-    # forces the length-L convolution into K channels run as one thread-block cluster
+@pytest.mark.parametrize("channel_mode", [1, 2])
+def test_channel_split_clusters(cuda, policy, max_len, channels, channel_mode):
+    # forces the length-L convolution into K channels, run as one
+    # thread-block cluster (1) or one after another in one CTA (2)
     g = np.random.default_rng(max_len)
     rows, cols = 123, 333
     coo = synthetic.normalise(rows, cols, g.integers(0, rows, 3000), g.integers(0, cols, 3000))
-    got, info = run_plan(coo, length_policy=policy, max_channel_len=max_len)
-    assert info["channels"] == channels
+    got, info = run_plan(coo, length_policy=policy, max_channel_len=max_len, channel_mode=channel_mode)
+    assert info["channels"] == channels and info["channel_mode"] == channel_mode
     check_against_oracle(coo, got)
+
+
+def test_channel_modes_agree_on_large_rows(cuda):
+    # 16706 columns need two channels; both layouts give the same spectrum
+    # to FP32 rounding
+    coo = synthetic.uniform_matrix(257, 16706, 40000, seed=12)
+    a, ia = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, channel_mode=1)
+    b, ib = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, channel_mode=2)
+    assert ia["channels"] == 2 and ib["channel_mode"] == 2
+    assert fp64.rel_l2(a, b) < 1e-6
+    check_against_oracle(coo, b, us=np.array([0, 1, 77, 128, 256]))
 
 
 def test_u_tiles_and_index_width(cuda):

@@ -58,10 +58,11 @@ def test_streaming_bit_identical_on_256_row_tiles(cuda, policy):
     assert np.array_equal(streamed(coo, 512, pinned=False, length_policy=policy), want)
 
 
-def test_streaming_cluster_plan(cuda):
-    # convolution split over 3 channels (thread-block clusters)
+@pytest.mark.parametrize("channel_mode", [1, 2])
+def test_streaming_cluster_plan(cuda, channel_mode):
+    # convolution split over 3 channels (clusters, or sequential in one CTA)
     coo = synthetic.uniform_matrix(700, 333, 5000, seed=4)
-    got = streamed(coo, 64, length_policy=gb.GBSP_LEN_7SMOOTH, max_channel_len=250)
+    got = streamed(coo, 64, length_policy=gb.GBSP_LEN_7SMOOTH, max_channel_len=250, channel_mode=channel_mode)
     ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx)
     assert fp64.rel_l2(got[:, :coo.cols // 2 + 1], ref) <= 1e-5
 
