@@ -28,10 +28,18 @@ __device__ __forceinline__ uint32_t mod_magic(uint32_t x, uint32_t n, uint32_t m
     return ((int32_t)r < 0) ? r + n : r;
 }
 
-// (u*r) mod rows; BIG handles rows > 65535 where u*r may not fit 32 bits.
+// (u*r) mod rows; BIG handles rows > 65535 where u*r may not fit 32 bits:
+// the 64-bit product is reduced with magic = ceil(2^64 / rows) as the
+// 32-bit case is (u, r < rows < 2^31 keep the quotient estimate within one).
 template <bool BIG>
-__device__ __forceinline__ uint32_t mulmod_rows(uint32_t u, uint32_t r, uint32_t rows, uint32_t magic) {
-    if (BIG) return (uint32_t)(((uint64_t)u * (uint64_t)r) % (uint64_t)rows);
+__device__ __forceinline__ uint32_t mulmod_rows(uint32_t u, uint32_t r, uint32_t rows, uint32_t magic,
+                                                unsigned long long magic64) {
+    if (BIG) {
+        const unsigned long long x = (unsigned long long)u * r;
+        const unsigned long long q = __umul64hi(x, magic64);
+        const long long rem = (long long)(x - q * rows);
+        return (uint32_t)(rem < 0 ? rem + rows : rem);
+    }
     return mod_magic(u * r, rows, magic);
 }
 
@@ -41,12 +49,14 @@ __device__ __forceinline__ uint32_t mulmod_rows(uint32_t u, uint32_t r, uint32_t
 // ---------------------------------------------------------------------------
 
 // tab[p] = exp(-2*pi*i*p/rows), p < ntab
-__global__ void k_table_rows(float2* __restrict__ tab, int ntab, int rows) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= ntab) return;
+// two_level: entries TWO_LO.. hold W^(TWO_LO*j) (layout of TAB_TWO)
+__global__ void k_table_rows(float2* __restrict__ tab, int ntab, int rows, int two_level) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntab) return;
+    const long long p = (two_level && i >= TWO_LO) ? (long long)(i - TWO_LO) * TWO_LO % rows : i;
     double s, c;
     sincospi(-2.0 * (double)p / (double)rows, &s, &c);
-    tab[p] = make_float2((float)c, (float)s);
+    tab[i] = make_float2((float)c, (float)s);
 }
 
 // Chirp exp(-i*pi*c^2/cols) times W_L^{+c*q} (sign = +1) or W_L^{-c*q} (sign = -1),
@@ -242,9 +252,15 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 // output row per thread, and writes strided 8-byte values
 // (src/sparse_fft_bluestein.cu:366-397).
 // ---------------------------------------------------------------------------
-template <bool TAB_HALF>
+// Pass-1 row twiddle tables in shared memory (TAB):
+//   TAB_FULL   tab[p] = W^p, p < rows
+//   TAB_HALF   tab[p] = W^p, p <= rows/2; the rest by conjugate symmetry
+//   TAB_TWO    two levels for tall matrices: tab[i] = W^i (i < TWO_LO),
+//              tab[TWO_LO + j] = W^(TWO_LO*j); W^p = hi[p / TWO_LO] * lo[p % TWO_LO]
+template <int TAB>
 __device__ __forceinline__ float2 row_twiddle(const float2* tab, uint32_t p, uint32_t rows, uint32_t hr) {
-    if (!TAB_HALF) return tab[p];
+    if (TAB == TAB_FULL) return tab[p];
+    if (TAB == TAB_TWO) return cmul(tab[TWO_LO + (p >> TWO_LO_BITS)], tab[p & (TWO_LO - 1)]);
     bool hi = p > hr;
     float2 w = tab[hi ? rows - p : p];
     w.y = hi ? -w.y : w.y;
@@ -257,10 +273,11 @@ struct NzInfo {
     float wx, wy;
 };
 
-template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU>
 __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx, int beg, int end,
                                                  const float2* tab, NzInfo* info, uint32_t u_lane,
-                                                 uint32_t rows, uint32_t magic, int lane, bool compensated,
+                                                 uint32_t rows, uint32_t magic, unsigned long long magic64,
+                                                 int lane, bool compensated,
                                                  float2 (&acc)[KU]) {
     float2 cmp[KU];
 #pragma unroll
@@ -270,9 +287,9 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
         const int cnt = min(32, end - p0);
         if (lane < cnt) {
             const uint32_t r = (uint32_t)row_idx[p0 + lane];
-            const uint32_t d = mulmod_rows<BIG>(32u, r, rows, magic);
-            const float2 wd = row_twiddle<TAB_HALF>(tab, d, rows, hr);
-            const uint32_t st = (KU > P1_RESEED) ? mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic) : 0u;
+            const uint32_t d = mulmod_rows<BIG>(32u, r, rows, magic, magic64);
+            const float2 wd = row_twiddle<TAB>(tab, d, rows, hr);
+            const uint32_t st = (KU > P1_RESEED) ? mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic, magic64) : 0u;
             info[lane] = NzInfo{r, st, wd.x, wd.y};
         }
         __syncwarp();
@@ -283,12 +300,12 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
         for (int i = 0; i < cnt; i++) {
             const NzInfo z = info[i];  // one broadcast 16-byte load
             const float2 wd = make_float2(z.wx, z.wy);
-            uint32_t p = mulmod_rows<BIG>(u_lane, z.r, rows, magic);
+            uint32_t p = mulmod_rows<BIG>(u_lane, z.r, rows, magic, magic64);
             float2 w = make_float2(1.f, 0.f);
 #pragma unroll
             for (int kk = 0; kk < KU; kk++) {
                 if (kk % P1_RESEED == 0) {
-                    w = row_twiddle<TAB_HALF>(tab, p, rows, hr);
+                    w = row_twiddle<TAB>(tab, p, rows, hr);
                     if (kk + P1_RESEED < KU) {
                         const uint32_t pn = p + z.step;
                         p = min(pn, pn - rows);
@@ -336,6 +353,7 @@ struct P1Args {
     size_t s_pitch;
     int cw, cols, s_cols, ntab, rows, u0, tile_rows, kahan_min;
     uint32_t magic;
+    unsigned long long magic64;  // ceil(2^64 / rows), for rows > 65535
 };
 
 struct P1Shared {
@@ -351,7 +369,7 @@ __device__ __forceinline__ long p1_items(const P1Args& a, int ublk) {
 // Work item `it` of one matrix: all tasks of one (row block, column window),
 // then the window's tile written to S.  Whole CTA; tab holds the matrix's
 // twiddle table.
-template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU>
 __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage, NzInfo* info_all,
                                         const float2* tab, P1Shared& sh) {
     constexpr int UBLK = 32 * KU;
@@ -380,8 +398,8 @@ __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage,
         const int2 range = a.win_task[(size_t)w * vmax + i];
         const int col = a.win_task_col[(size_t)w * vmax + i];
         float2 acc[KU];
-        column_sums_warp<IDX, TAB_HALF, BIG, KU>(row_idx, range.x, range.y, tab, info, u_lane,
-                                                 (uint32_t)a.rows, a.magic, lane,
+        column_sums_warp<IDX, TAB, BIG, KU>(row_idx, range.x, range.y, tab, info, u_lane,
+                                                 (uint32_t)a.rows, a.magic, a.magic64, lane,
                                                  a.kahan_min > 0 && range.y - range.x >= a.kahan_min, acc);
 #pragma unroll
         for (int kk = 0; kk < KU; kk++) stage[(lane + 32 * kk) * pitch + col] = acc[kk];
@@ -416,7 +434,7 @@ __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage,
     __syncthreads();
 }
 
-template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU>
 __global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
     extern __shared__ float4 smem_raw[];
     __shared__ P1Shared sh;
@@ -428,7 +446,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
     __syncthreads();
     const long nitems = p1_items(a, 32 * KU);
     for (long it = blockIdx.x; it < nitems; it += gridDim.x)
-        p1_item<IDX, TAB_HALF, BIG, KU>(a, it, stage, info_all, tab, sh);
+        p1_item<IDX, TAB, BIG, KU>(a, it, stage, info_all, tab, sh);
 }
 
 // Batched pass 1: the work items of many matrices (item_begin: first item of
@@ -436,7 +454,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
 // one item per grab.  Items are grabbed in increasing order, so a CTA moves
 // forward through the matrices and reloads the twiddle table only when it
 // enters a new one.  *queue must be 0 at launch.
-template <typename IDX, bool TAB_HALF, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU>
 __global__ void __launch_bounds__(P1_THREADS, 1)
 k_twiddle_sum_batch(const P1Args* __restrict__ args, const long* __restrict__ item_begin, int nmat,
                     unsigned long long* queue) {
@@ -473,7 +491,7 @@ k_twiddle_sum_batch(const P1Args* __restrict__ args, const long* __restrict__ it
         }
         NzInfo* info_all = reinterpret_cast<NzInfo*>(stage + (size_t)32 * KU * p1_pitch(cur.cw));
         float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
-        p1_item<IDX, TAB_HALF, BIG, KU>(cur, it - item_begin[m], stage, info_all, tab, sh);
+        p1_item<IDX, TAB, BIG, KU>(cur, it - item_begin[m], stage, info_all, tab, sh);
     }
 }
 

@@ -25,6 +25,9 @@ GBSP_HD constexpr int p1_pitch(int cw) { return p1_vmax(cw) + 1; }
 GBSP_HD constexpr size_t p1_head_bytes(int ku, int cw) {
     return (size_t)32 * ku * p1_pitch(cw) * 8 + (size_t)P1_WARPS * 32 * 16;
 }
+// pass-1 twiddle table layouts (see row_twiddle)
+constexpr int TAB_FULL = 0, TAB_HALF = 1, TAB_TWO = 2;
+constexpr int TWO_LO_BITS = 8, TWO_LO = 1 << TWO_LO_BITS;
 constexpr long long WAIT_LIMIT = 1LL << 26;  // bounded spin on an mbarrier (~seconds)
 constexpr int ERR_TIMEOUT = 1;              // bit set in the plan's error word
 constexpr int ERR_RADIX = 2;                // a stage radix the kernel was not compiled for

@@ -33,11 +33,12 @@ struct gbsp_plan_s {
     int L = 0, K = 1, Lp = 0;
     gbsp::FFTDesc fd{};
     int half_rows = 0, u_tile = 0, out_cols = 0, out_pitch = 0;
-    int idx_bytes = 2, tab_half = 0, big = 0, kahan_min = 64, ntab = 0;
+    int idx_bytes = 2, tab_mode = 0, big = 0, kahan_min = 64, ntab = 0;  // tab_mode: gbsp::TAB_*
     int p1_ku = 8, p1_cw = 32;       // pass-1 rows per lane (x32 per item) and window width
-    int p1_shape = 1;                // 1-based index of (p1_ku, p1_cw, tab_half) in the shape table
+    int p1_shape = 1;                // 1-based index of (p1_ku, p1_cw, tab_mode) in the shape table
     int planner = GBSP_PLANNER_MODEL;
     uint32_t rows_magic = 0;
+    unsigned long long rows_magic64 = 0;  // ceil(2^64 / rows)
     void* d_row_idx = nullptr;       // nnz, u16 or u32, column order
     uint8_t* d_win_slot0 = nullptr;  // pass-1 windows: first tile column of each column
     int2* d_win_task = nullptr;      // pass-1 windows: nonzero range of each task
@@ -149,9 +150,9 @@ void free_plan(gbsp_plan_s* p) {
 
 inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-template <typename IDX, bool HALF, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU>
 int p1_prepare(gbsp_plan_s* p, int sms) {
-    auto kern = gbsp::k_twiddle_sum<IDX, HALF, BIG, KU>;
+    auto kern = gbsp::k_twiddle_sum<IDX, TAB, BIG, KU>;
     if (int rc = allow_full_smem(kern)) return rc;
     int nb = 0;
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, gbsp::P1_THREADS, p->p1_smem));
@@ -179,43 +180,47 @@ gbsp::P1Args p1_args(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pi
     a.tile_rows = n;
     a.kahan_min = p->kahan_min;
     a.magic = p->rows_magic;
+    a.magic64 = p->rows_magic64;
     return a;
 }
 
-template <typename IDX, bool HALF, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU>
 void p1_launch(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pitch, const float2* chirp,
                cudaStream_t st) {
-    gbsp::k_twiddle_sum<IDX, HALF, BIG, KU><<<p->p1_grid, gbsp::P1_THREADS, p->p1_smem, st>>>(
+    gbsp::k_twiddle_sum<IDX, TAB, BIG, KU><<<p->p1_grid, gbsp::P1_THREADS, p->p1_smem, st>>>(
         p1_args(p, u0, n, S, s_pitch, chirp));
 }
 
 // prepare == true: set attributes and grid; false: launch
-template <typename IDX, bool HALF, bool BIG>
+template <typename IDX, int TAB, bool BIG>
 int p1_dispatch_ku(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
                    const float2* chirp, cudaStream_t st) {
     if (p->p1_ku == 8) {
-        if (prepare) return p1_prepare<IDX, HALF, BIG, 8>(p, sms);
-        p1_launch<IDX, HALF, BIG, 8>(p, u0, n, S, sp, chirp, st);
+        if (prepare) return p1_prepare<IDX, TAB, BIG, 8>(p, sms);
+        p1_launch<IDX, TAB, BIG, 8>(p, u0, n, S, sp, chirp, st);
     } else {
-        if (prepare) return p1_prepare<IDX, HALF, BIG, 4>(p, sms);
-        p1_launch<IDX, HALF, BIG, 4>(p, u0, n, S, sp, chirp, st);
+        if (prepare) return p1_prepare<IDX, TAB, BIG, 4>(p, sms);
+        p1_launch<IDX, TAB, BIG, 4>(p, u0, n, S, sp, chirp, st);
     }
     return GBSP_OK;
 }
 
 // 16-bit indices only occur with rows <= 65536 (no 64-bit phase products)
-template <bool HALF>
-int p1_dispatch_half(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
-                     const float2* chirp, cudaStream_t st) {
-    if (p->idx_bytes == 2) return p1_dispatch_ku<uint16_t, HALF, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
-    if (p->big) return p1_dispatch_ku<uint32_t, HALF, true>(p, prepare, sms, u0, n, S, sp, chirp, st);
-    return p1_dispatch_ku<uint32_t, HALF, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
+template <int TAB>
+int p1_dispatch_tab(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
+                    const float2* chirp, cudaStream_t st) {
+    if (p->idx_bytes == 2) return p1_dispatch_ku<uint16_t, TAB, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
+    if (p->big) return p1_dispatch_ku<uint32_t, TAB, true>(p, prepare, sms, u0, n, S, sp, chirp, st);
+    return p1_dispatch_ku<uint32_t, TAB, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
 }
 
 int p1_dispatch(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
                 const float2* chirp, cudaStream_t st) {
-    return p->tab_half ? p1_dispatch_half<true>(p, prepare, sms, u0, n, S, sp, chirp, st)
-                       : p1_dispatch_half<false>(p, prepare, sms, u0, n, S, sp, chirp, st);
+    switch (p->tab_mode) {
+        case gbsp::TAB_HALF: return p1_dispatch_tab<gbsp::TAB_HALF>(p, prepare, sms, u0, n, S, sp, chirp, st);
+        case gbsp::TAB_TWO: return p1_dispatch_tab<gbsp::TAB_TWO>(p, prepare, sms, u0, n, S, sp, chirp, st);
+        default: return p1_dispatch_tab<gbsp::TAB_FULL>(p, prepare, sms, u0, n, S, sp, chirp, st);
+    }
 }
 
 // chirp == nullptr gives the raw column sums (gbsp_column_sums)
@@ -409,7 +414,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     const size_t smem_cap = lim.smem_optin;
     const int sms = lim.sms;
     const int tmode = o.row_table_mode;
-    if (tmode < 0 || tmode > 2) return set_error(GBSP_ERR_INVALID, "row_table_mode must be 0, 1 or 2");
+    if (tmode < 0 || tmode > 3) return set_error(GBSP_ERR_INVALID, "row_table_mode must be 0, 1, 2 or 3");
     if (o.pass1_shape < 0 || o.pass1_shape > gbsp::N_P1_SHAPES)
         return set_error(GBSP_ERR_INVALID, "pass1_shape must be 0 (auto) or 1.." + std::to_string(gbsp::N_P1_SHAPES));
     if (o.planner != GBSP_PLANNER_MODEL && o.planner != GBSP_PLANNER_LEARNED)
@@ -445,6 +450,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->idx_bytes = ib;
     p->big = p->rows > 65535;
     p->rows_magic = (p->rows >= 2) ? (uint32_t)(((1ull << 32) + (uint64_t)p->rows - 1) / (uint64_t)p->rows) : 0u;
+    p->rows_magic64 = (p->rows >= 2) ? (unsigned long long)((((unsigned __int128)1 << 64) + p->rows - 1) / p->rows) : 0ull;
 
     // ---- pass-1 configuration: result tile + twiddle table in shared memory
     {
@@ -461,8 +467,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         p->p1_shape = idx + 1;
         p->p1_ku = sh.ku;
         p->p1_cw = sh.cw;
-        p->tab_half = sh.half;
-        p->ntab = sh.half ? p->rows / 2 + 1 : p->rows;
+        p->tab_mode = sh.tab;
+        p->ntab = (int)gbsp::row_table_entries(sh.tab, p->rows);
         p->p1_smem = gbsp::p1_smem_bytes(sh, p->rows);
     }
     if ((rc = p1_dispatch(p, true, sms, 0, 0, nullptr, 0, nullptr, st))) return rc;
@@ -573,7 +579,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     const int ntw = std::max(fft_tw_count(p->fd), 1);
     if ((rc = dev_alloc(p, (void**)&p->d_fftw, (size_t)ntw * sizeof(float2)))) return rc;
 
-    gbsp::k_table_rows<<<blocks_for(p->ntab, 256), 256, 0, st>>>(p->d_rowtab, p->ntab, p->rows);
+    gbsp::k_table_rows<<<blocks_for(p->ntab, 256), 256, 0, st>>>(p->d_rowtab, p->ntab, p->rows,
+                                                                 p->tab_mode == gbsp::TAB_TWO);
     GB_CUDA(cudaGetLastError());
     gbsp::k_table_pre<<<blocks_for((long)K * cols, 256), 256, 0, st>>>(p->d_pre, cols, p->L, K);
     GB_CUDA(cudaGetLastError());
@@ -667,7 +674,7 @@ int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
     info->half_rows = p->half_rows;
     info->u_tile = p->u_tile;
     info->index_bytes = p->idx_bytes;
-    info->row_table_mode = p->tab_half;
+    info->row_table_mode = p->tab_mode;
     info->rows_threads = p->rows_threads;
     info->device_bytes = p->device_bytes;
     info->pass1_shape = p->p1_shape;
@@ -845,7 +852,7 @@ struct gbsp_batch_s {
     std::vector<gbsp_plan_s*> plans;
     std::vector<int> order;      // queue order (batched matrices, costliest rows first)
     std::vector<int> separate;   // matrices that run through their own plan
-    int p1_shape = 1, ku = 8, cw = 32, half = 0, idx_bytes = 2, big = 0;
+    int p1_shape = 1, ku = 8, cw = 32, tab = 0, idx_bytes = 2, big = 0;
     int p1_grid = 0;
     size_t p1_smem = 0;
     // Row launches: one per class of matrices that share a block size and a
@@ -890,9 +897,9 @@ int batch_alloc(gbsp_batch_s* b, void** ptr, size_t bytes) {
     return GBSP_OK;
 }
 
-template <typename IDX, bool HALF, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU>
 int p1b_run(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    auto kern = gbsp::k_twiddle_sum_batch<IDX, HALF, BIG, KU>;
+    auto kern = gbsp::k_twiddle_sum_batch<IDX, TAB, BIG, KU>;
     if (prepare) {
         if (int rc = allow_full_smem(kern)) return rc;
         int nb = 0;
@@ -907,20 +914,24 @@ int p1b_run(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
     return GBSP_OK;
 }
 
-template <typename IDX, bool HALF, bool BIG>
+template <typename IDX, int TAB, bool BIG>
 int p1b_ku(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    return b->ku == 8 ? p1b_run<IDX, HALF, BIG, 8>(b, prepare, sms, st) : p1b_run<IDX, HALF, BIG, 4>(b, prepare, sms, st);
+    return b->ku == 8 ? p1b_run<IDX, TAB, BIG, 8>(b, prepare, sms, st) : p1b_run<IDX, TAB, BIG, 4>(b, prepare, sms, st);
 }
 
-template <bool HALF>
-int p1b_half(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    if (b->idx_bytes == 2) return p1b_ku<uint16_t, HALF, false>(b, prepare, sms, st);
-    if (b->big) return p1b_ku<uint32_t, HALF, true>(b, prepare, sms, st);
-    return p1b_ku<uint32_t, HALF, false>(b, prepare, sms, st);
+template <int TAB>
+int p1b_tab(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
+    if (b->idx_bytes == 2) return p1b_ku<uint16_t, TAB, false>(b, prepare, sms, st);
+    if (b->big) return p1b_ku<uint32_t, TAB, true>(b, prepare, sms, st);
+    return p1b_ku<uint32_t, TAB, false>(b, prepare, sms, st);
 }
 
 int p1b_dispatch(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    return b->half ? p1b_half<true>(b, prepare, sms, st) : p1b_half<false>(b, prepare, sms, st);
+    switch (b->tab) {
+        case gbsp::TAB_HALF: return p1b_tab<gbsp::TAB_HALF>(b, prepare, sms, st);
+        case gbsp::TAB_TWO: return p1b_tab<gbsp::TAB_TWO>(b, prepare, sms, st);
+        default: return p1b_tab<gbsp::TAB_FULL>(b, prepare, sms, st);
+    }
 }
 
 int batch_launch(gbsp_batch_s* b, cudaStream_t st) {
@@ -991,7 +1002,7 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
         b->p1_shape = fit[0] + 1;
         b->ku = gbsp::kP1Shapes[fit[0]].ku;
         b->cw = gbsp::kP1Shapes[fit[0]].cw;
-        b->half = gbsp::kP1Shapes[fit[0]].half;
+        b->tab = gbsp::kP1Shapes[fit[0]].tab;
         b->p1_smem = gbsp::p1_smem_bytes(gbsp::kP1Shapes[fit[0]], max_rows);
     }
     // one plan per matrix with the common pass-1 shape; row blocks of 256 or

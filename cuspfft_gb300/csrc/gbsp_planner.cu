@@ -174,21 +174,35 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
 }
 
 // Preference order: 256-row items with 32-column windows, full table, then
-// half table; then 128-row items with 64- or 32-column windows.
-const P1Shape kP1Shapes[N_P1_SHAPES] = {{8, 32, 0}, {8, 32, 1}, {4, 64, 0}, {4, 32, 0}, {4, 64, 1}, {4, 32, 1}};
+// half table; then 128-row items with 64- or 32-column windows; last the
+// two-level tables for matrices too tall for either.
+const P1Shape kP1Shapes[N_P1_SHAPES] = {{8, 32, TAB_FULL}, {8, 32, TAB_HALF}, {4, 64, TAB_FULL}, {4, 32, TAB_FULL},
+                                        {4, 64, TAB_HALF}, {4, 32, TAB_HALF}, {8, 32, TAB_TWO},  {4, 32, TAB_TWO}};
+
+size_t row_table_entries(int tab, int rows) {
+    if (tab == TAB_HALF) return (size_t)(rows / 2 + 1);
+    if (tab == TAB_TWO) return (size_t)TWO_LO + (size_t)(rows + TWO_LO - 1) / TWO_LO;
+    return (size_t)rows;
+}
 
 size_t p1_smem_bytes(const P1Shape& sh, int rows) {
-    const size_t ntab = sh.half ? (size_t)(rows / 2 + 1) : (size_t)rows;
-    return p1_head_bytes(sh.ku, sh.cw) + ntab * 8;
+    return p1_head_bytes(sh.ku, sh.cw) + row_table_entries(sh.tab, rows) * 8;
 }
 
 std::vector<int> fitting_p1_shapes(int rows, size_t smem_cap, int table_mode) {
     std::vector<int> out;
-    for (int i = 0; i < N_P1_SHAPES; i++) {
-        const P1Shape& sh = kP1Shapes[i];
-        if ((table_mode == 1 && sh.half) || (table_mode == 2 && !sh.half)) continue;
-        if (p1_smem_bytes(sh, rows) + 1024 > smem_cap) continue;  // + static shared variables
-        out.push_back(i);
+    for (int pass = 0; pass < 2 && out.empty(); pass++) {
+        for (int i = 0; i < N_P1_SHAPES; i++) {
+            const P1Shape& sh = kP1Shapes[i];
+            const bool two = sh.tab == TAB_TWO;
+            if (table_mode == 0 && two != (pass == 1)) continue;
+            if (table_mode == 1 && sh.tab != TAB_FULL) continue;
+            if (table_mode == 2 && sh.tab != TAB_HALF) continue;
+            if (table_mode == 3 && !two) continue;
+            if (p1_smem_bytes(sh, rows) + 1024 > smem_cap) continue;  // + static shared variables
+            out.push_back(i);
+        }
+        if (table_mode != 0) break;
     }
     return out;
 }
@@ -295,8 +309,9 @@ int plan_features(int rows, int cols, int n_active, int nnz, const int* col_ptr,
     f[26] = (float)std::max(1, std::min({(int)(233472 / (rows_smem_bytes(fd) + 1024)), 2048 / rp.nt,
                                          65536 / (rp.nt * regs)}));
     f[27] = lg2(rp.cost);
-    // pass-1 shape
-    f[28 + sh_idx] = 1.f;
+    // pass-1 shape (the two-level shapes share the slot of their half-table
+    // twin: the model never saw them, and they only appear when nothing else fits)
+    f[28 + (sh_idx == 6 ? 1 : sh_idx == 7 ? 5 : sh_idx)] = 1.f;
     const int s_cols = (cols + 1) & ~1;
     const double items = std::ceil(half_rows / (32.0 * sh.ku)) * std::ceil((double)s_cols / sh.cw);
     f[34] = lg2(items);

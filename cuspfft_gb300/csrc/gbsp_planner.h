@@ -35,15 +35,18 @@ struct ChannelSplit {
 };
 int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSplit* out);
 
-// ---- pass 1 shapes: {rows per lane, window width, half twiddle table}
+// ---- pass 1 shapes: {rows per lane, window width, twiddle table layout
+// (TAB_FULL, TAB_HALF, TAB_TWO)}
 struct P1Shape {
-    int ku, cw, half;
+    int ku, cw, tab;
 };
-constexpr int N_P1_SHAPES = 6;
+constexpr int N_P1_SHAPES = 8;
 extern const P1Shape kP1Shapes[N_P1_SHAPES];
+size_t row_table_entries(int tab, int rows);
 size_t p1_smem_bytes(const P1Shape& sh, int rows);
 // Indices (0-based, preference order) of the shapes that fit for `rows`
-// under the table mode (0 auto, 1 full, 2 half).
+// under the table mode (0 auto, 1 full, 2 half, 3 two-level).  Auto offers
+// the two-level shapes only when no full or half table fits.
 std::vector<int> fitting_p1_shapes(int rows, size_t smem_cap, int table_mode);
 
 // Shared memory per CTA available to the kernels: the current device's

@@ -56,8 +56,9 @@ enum { GBSP_PLANNER_MODEL = 0, GBSP_PLANNER_LEARNED = 1 };
 /* Pass-1 shapes (gbsp_options.pass1_shape, 1-based):
  *   1: 256 rows x 32-column windows, full twiddle table
  *   2: 256 x 32, half table      3: 128 x 64, full    4: 128 x 32, full
- *   5: 128 x 64, half            6: 128 x 32, half */
-#define GBSP_N_PASS1_SHAPES 6
+ *   5: 128 x 64, half            6: 128 x 32, half
+ *   7: 256 x 32, two-level       8: 128 x 32, two-level (tall matrices) */
+#define GBSP_N_PASS1_SHAPES 8
 /* Length of the cost-model feature vector (gbsp_plan_features). */
 #define GBSP_N_FEATURES 36
 
@@ -78,7 +79,8 @@ typedef struct {
     int rows_threads;      /* row-kernel block size: 0 = auto, else a multiple of 32
                               in [64, 1024] (at most 512 when a radix exceeds 16)         */
     int row_table_mode;    /* pass-1 twiddle table: 0 = auto, 1 = full circle,
-                              2 = half circle (smaller, more blocks per SM)               */
+                              2 = half circle, 3 = two-level (W^p = hi[p/256]*lo[p%256],
+                              any row count; auto uses it only when no other fits)       */
     int radix[8];          /* channel FFT radix per stage, first to last, 0-terminated;
                               all zero = auto.  Allowed: 2 3 4 5 7 8 9 12 15 16 20 21
                               24 25 28 32 35 40; product = channel length                 */
@@ -104,7 +106,7 @@ typedef struct {
     int half_rows;         /* rows/2 + 1 Bluestein rows (Hermitian pairing)              */
     int u_tile;            /* effective Bluestein rows per tile                           */
     int index_bytes;       /* 2 or 4                                                      */
-    int row_table_mode;    /* 0 full twiddle table in shared memory, 1 half table        */
+    int row_table_mode;    /* pass-1 table in shared memory: 0 full, 1 half, 2 two-level  */
     int rows_threads;      /* row-kernel block size in use                                */
     size_t device_bytes;   /* device memory held by the plan                              */
     int pass1_shape;       /* pass-1 shape in use (1-based)                               */

@@ -224,3 +224,26 @@ def test_cli_methods_with_host_reference(cuda, tmp_path):
         max_rel = float(ln.split("max_rel")[1].split()[0])
         assert max_rel < 1e-4, ln
     assert "n=3" in res.stdout
+
+
+@pytest.mark.parametrize("rows,cols,index_bytes", [(60001, 40, 0), (70001, 64, 0), (131071, 33, 4)])
+def test_tall_matrices_two_level_table(cuda, rows, cols, index_bytes):
+    # too many rows for a full or half twiddle table in shared memory: pass 1
+    # reads W^p as hi[p / 256] * lo[p % 256]; above 65535 rows the phases use
+    # 64-bit products
+    g = np.random.default_rng(rows)
+    n = 3 * rows
+    coo = synthetic.normalise(rows, cols, g.integers(0, rows, n), g.integers(0, cols, n))
+    got, info = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, index_bytes=index_bytes)
+    assert info["row_table_mode"] == 2
+    us = np.unique(np.r_[0:4, rows // 3, rows // 2 - 1:rows // 2 + 2, rows - 3:rows] % rows)
+    check_against_oracle(coo, got, us=us)
+
+
+def test_two_level_table_on_request(cuda):
+    coo = synthetic.uniform_matrix(3001, 2048, 30730, seed=1)
+    full, _ = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, row_table_mode=1)
+    two, info = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, row_table_mode=3)
+    assert info["row_table_mode"] == 2 and info["pass1_shape"] in (7, 8)
+    assert fp64.rel_l2(two, full) < 1e-6
+    check_against_oracle(coo, two)
