@@ -545,7 +545,9 @@ struct RowsArgs {
 //               cluster; the output combine reads the peers' buffers (DSMEM)
 //   ROW_SEQ     one CTA runs the K channels one after another; the first K-1
 //               results wait in an L2-resident scratch for the combine
-constexpr int ROW_SINGLE = 0, ROW_CLUSTER = 1, ROW_SEQ = 2;
+//   ROW_SEQW    ROW_SEQ for more than MAX_CHANNELS channels (very wide rows;
+//               a separate instance, so the common one keeps its registers)
+constexpr int ROW_SINGLE = 0, ROW_CLUSTER = 1, ROW_SEQ = 2, ROW_SEQW = 3;
 
 // One Bluestein row t of the tile (u = u0 + t), channel q of K: input,
 // forward network, filter, inverse network, Hermitian-paired output.  Whole
@@ -557,6 +559,7 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                                               uint32_t& parity, int& err_bits) {
     constexpr bool CLUSTER = MODE == ROW_CLUSTER;
     constexpr bool MULTI = MODE != ROW_SINGLE;
+    constexpr bool SEQ = MODE == ROW_SEQ || MODE == ROW_SEQW;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int Lp = fd.Lp, K = a.K, cols = a.cols;
     const int half_slots = (int)(a.out_pitch >> 1);
@@ -570,8 +573,8 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     const float2* srow = a.S + (size_t)t * a.s_pitch;
     bool ok = true;
     // ROW_SEQ runs every channel of the row here; the other modes one
-    const int q_end = (MODE == ROW_SEQ) ? K : q + 1;
-    for (int qc = (MODE == ROW_SEQ) ? 0 : q; qc < q_end; qc++) {
+    const int q_end = SEQ ? K : q + 1;
+    for (int qc = SEQ ? 0 : q; qc < q_end; qc++) {
         const float2* preq = a.pre + (size_t)qc * cols;
         const float2* filtq = a.filt + (size_t)qc * Lp;
         // (a single channel always has cols_even <= Lp: L >= 2*cols - 1)
@@ -586,6 +589,23 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
             parity ^= 1u;
             if (MULTI && qc != 0)  // channel pre-twiddle (channel 0's is 1)
                 for (int c = tid; c < cols; c += nt) buf[c] = cmul(buf[c], __ldg(preq + c));
+            __syncthreads();
+        } else if constexpr (MODE == ROW_SEQW) {
+            // Several input columns fold onto one slot: slot n gets
+            // sum_j pre[n + j*Lp] * x[n + j*Lp], up to K/2 + 1 sections
+            // (very wide rows, K up to MAX_SEQ_CHANNELS); loads of two
+            // sections per step
+            for (int n = tid; n < Lp; n += nt) {
+                float2 acc = make_float2(0.f, 0.f);
+                for (int c = n; c < cols; c += 2 * Lp) {
+                    const int c2 = c + Lp;
+                    const float2 x0 = __ldcs(srow + c), p0 = __ldg(preq + c);
+                    const float2 x1 = (c2 < cols) ? __ldcs(srow + c2) : make_float2(0.f, 0.f);
+                    const float2 p1 = (c2 < cols) ? __ldg(preq + c2) : make_float2(0.f, 0.f);
+                    acc = cadd(acc, cadd(cmul(x0, p0), cmul(x1, p1)));
+                }
+                buf[n] = acc;
+            }
             __syncthreads();
         } else if constexpr (MULTI) {
             // Several input columns fold onto one slot: slot n gets
@@ -625,7 +645,7 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                                               (const float2*)nullptr, tid, nt);
             __syncthreads();
         }
-        if (MODE == ROW_SEQ && qc < K - 1) {  // park the channel for the combine
+        if (SEQ && qc < K - 1) {  // park the channel for the combine
             float2* dst = a.zscratch + ((size_t)blockIdx.x * (K - 1) + qc) * Lp;
             for (int i = tid; i < Lp; i += nt) dst[i] = buf[i];
             __syncthreads();
@@ -694,8 +714,16 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                     const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
                     int n = c;
                     while (n >= Lp) n -= Lp;
-                    for (int qq = 0; qq < K; qq++)
-                        val = cadd(val, cmul(zsrc[qq][n], __ldg(a.post + (size_t)qq * cols + c)));
+                    if constexpr (MODE == ROW_SEQW) {
+                        // channels 0..K-2 wait in this CTA's scratch, K-1 in buf
+                        const float2* zs = a.zscratch + (size_t)blockIdx.x * (K - 1) * Lp + n;
+                        for (int qq = 0; qq < K - 1; qq++)
+                            val = cadd(val, cmul(zs[(size_t)qq * Lp], __ldg(a.post + (size_t)qq * cols + c)));
+                        val = cadd(val, cmul(buf[n], __ldg(a.post + (size_t)(K - 1) * cols + c)));
+                    } else {
+                        for (int qq = 0; qq < K; qq++)
+                            val = cadd(val, cmul(zsrc[qq][n], __ldg(a.post + (size_t)qq * cols + c)));
+                    }
                     if (sel) val.y = -val.y;
                 }
                 o[e] = val;
@@ -724,7 +752,7 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
 
     constexpr int MAXR = (NTMAX > 512) ? MAX_RADIX_NT1024 : MAX_RADIX_NT512;
     int q = 0, cid = blockIdx.x, ncl = gridDim.x;
-    const float2* zsrc[MODE == ROW_SINGLE ? 1 : MAX_CHANNELS];
+    const float2* zsrc[(MODE == ROW_CLUSTER || MODE == ROW_SEQ) ? MAX_CHANNELS : 1];
     if constexpr (MODE == ROW_CLUSTER) {
         const int K = a.K;
         cg::cluster_group cl = cg::this_cluster();
@@ -735,6 +763,8 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
         for (int i = 0; i < MAX_CHANNELS; i++)
             zsrc[i] = (i < K) ? cl.map_shared_rank(buf, i) : buf;
     } else if constexpr (MODE == ROW_SEQ) {
+        // channels 0..K-2 wait in this CTA's scratch, K-1 in buf (K > MAX_CHANNELS
+        // computes the pointers as it goes)
         const int K = a.K;
 #pragma unroll
         for (int i = 0; i < MAX_CHANNELS; i++)

@@ -13,7 +13,8 @@
 namespace gbsp {
 
 constexpr int MAX_STAGES = 16;
-constexpr int MAX_CHANNELS = 8;
+constexpr int MAX_CHANNELS = 8;       // channels a thread-block cluster can hold
+constexpr int MAX_SEQ_CHANNELS = 64;  // channels one CTA runs in turn (very wide matrices)
 constexpr int P1_THREADS = 512;     // k_twiddle_sum block size
 constexpr int P1_WARPS = P1_THREADS / 32;
 constexpr int P1_RESEED = 4;        // exact table lookup every P1_RESEED rows

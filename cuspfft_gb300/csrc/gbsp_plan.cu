@@ -319,8 +319,10 @@ int launch_rows_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t
             return n512 ? rows_launch_args<ROW_SINGLE, 512>(p, a, st) : rows_launch_args<ROW_SINGLE, 1024>(p, a, st);
         case ROW_CLUSTER:
             return n512 ? rows_launch_args<ROW_CLUSTER, 512>(p, a, st) : rows_launch_args<ROW_CLUSTER, 1024>(p, a, st);
-        default:
+        case ROW_SEQ:
             return rows_launch_args<ROW_SEQ, 512>(p, a, st);
+        default:
+            return rows_launch_args<ROW_SEQW, 512>(p, a, st);
     }
 }
 
@@ -340,6 +342,10 @@ int rows_prepare(gbsp_plan_s* p, int sms) {
     using namespace gbsp;
     if (p->K == 1) p->row_mode = ROW_SINGLE;
     else if (p->row_mode != ROW_SEQ || p->rows_ntmax != 512) p->row_mode = ROW_CLUSTER;
+    if (p->row_mode == ROW_CLUSTER && p->K > MAX_CHANNELS)
+        return set_error(GBSP_ERR_UNSUPPORTED, "more than " + std::to_string(MAX_CHANNELS) +
+                                                   " channels need sequential channels (512-thread rows)");
+    if (p->row_mode == ROW_SEQ && p->K > MAX_CHANNELS) p->row_mode = ROW_SEQW;
     int cap = 0, rc;
     const bool n512 = p->rows_ntmax == 512;
     switch (p->row_mode) {
@@ -349,8 +355,11 @@ int rows_prepare(gbsp_plan_s* p, int sms) {
         case ROW_CLUSTER:
             rc = n512 ? rows_capacity<ROW_CLUSTER, 512>(p, sms, &cap) : rows_capacity<ROW_CLUSTER, 1024>(p, sms, &cap);
             break;
-        default:
+        case ROW_SEQ:
             rc = rows_capacity<ROW_SEQ, 512>(p, sms, &cap);
+            break;
+        default:
+            rc = rows_capacity<ROW_SEQW, 512>(p, sms, &cap);
     }
     if (rc) return rc;
     if (cap < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row kernel does not fit on an SM");
@@ -527,7 +536,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
                                 (size_t)ntw_all * sizeof(float2), (size_t)p->K * p->Lp * sizeof(double2),
                                 (size_t)p->K * p->Lp * sizeof(double2),
                                 (size_t)p->u_tile * s_pitch_all * sizeof(float2),
-                                (p->row_mode == gbsp::ROW_SEQ)
+                                (p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW)
                                     ? (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2)
                                     : 0};
         size_t total = 0;
@@ -546,7 +555,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         p->arena_off = 0;
     }
     if ((rc = dev_alloc(p, (void**)&p->d_win_slot0, slot0.size()))) return rc;
-    if (p->row_mode == gbsp::ROW_SEQ &&
+    if ((p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW) &&
         (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2))))
         return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_win_task, task.size() * sizeof(int2)))) return rc;
@@ -679,7 +688,7 @@ int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
     info->device_bytes = p->device_bytes;
     info->pass1_shape = p->p1_shape;
     info->planner = p->planner;
-    info->channel_mode = p->K == 1 ? 0 : (p->row_mode == gbsp::ROW_SEQ ? 2 : 1);
+    info->channel_mode = p->K == 1 ? 0 : (p->row_mode == gbsp::ROW_CLUSTER ? 1 : 2);
     return GBSP_OK;
 }
 

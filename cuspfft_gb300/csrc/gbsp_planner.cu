@@ -159,7 +159,9 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
     const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 24000;
     out->L = (int)L;
     out->K = 0;
-    for (int k = 1; k <= MAX_CHANNELS; k++) {
+    // more than MAX_CHANNELS channels only run sequentially in one CTA
+    const int kmax = (o && o->channel_mode == 1) ? MAX_CHANNELS : MAX_SEQ_CHANNELS;
+    for (int k = 1; k <= kmax; k++) {
         if (L % k || L / k > maxLp || L / k < 2) continue;
         auto ranked = rank_radices((int)(L / k), smem_cap, o ? o->radix : nullptr, nt_opt);
         if (ranked.empty()) continue;
@@ -169,7 +171,7 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
         return GBSP_OK;
     }
     return set_error(GBSP_ERR_UNSUPPORTED, "fft_len " + std::to_string(L) + " does not split into <= " +
-                                               std::to_string(MAX_CHANNELS) + " channels of <= " +
+                                               std::to_string(kmax) + " channels of <= " +
                                                std::to_string(maxLp) + " that fit in shared memory");
 }
 

@@ -27,7 +27,8 @@ struct RadixPlan {
 // null) and nt_opt (0 = automatic: 256 or 512) restrict the set.
 std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt);
 
-// Channel split of the length-L convolution: the smallest K (<= MAX_CHANNELS)
+// Channel split of the length-L convolution: the smallest K (<= MAX_CHANNELS
+// for clusters, MAX_SEQ_CHANNELS for sequential channels)
 // whose channel length fits; ranked radix choices for that channel.
 struct ChannelSplit {
     int L = 0, K = 0, Lp = 0;

@@ -247,3 +247,17 @@ def test_two_level_table_on_request(cuda):
     assert info["row_table_mode"] == 2 and info["pass1_shape"] in (7, 8)
     assert fp64.rel_l2(two, full) < 1e-6
     check_against_oracle(coo, two)
+
+
+@pytest.mark.parametrize("rows,cols", [(33, 120001), (5, 200003)])
+def test_wide_matrices_many_channels(cuda, rows, cols):
+    # the convolution needs more channels than a cluster holds (L > 8 x 24000):
+    # one CTA runs them in turn
+    g = np.random.default_rng(cols)
+    n = 4 * cols
+    coo = synthetic.normalise(rows, cols, g.integers(0, rows, n), g.integers(0, cols, n))
+    got, info = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH)
+    assert info["channels"] > 8 and info["channel_mode"] == 2
+    check_against_oracle(coo, got)
+    with pytest.raises(gb.GbspError):
+        gb.Plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, channel_mode=1)
