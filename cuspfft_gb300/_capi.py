@@ -54,7 +54,7 @@ class GbspOptions(C.Structure):
         ("pass1_shape", C.c_int),
         ("planner", C.c_int),
         ("channel_mode", C.c_int),
-        ("reserved", C.c_int * 1),
+        ("stream_tile_rows", C.c_int),
     ]
 
     def radices(self) -> tuple:

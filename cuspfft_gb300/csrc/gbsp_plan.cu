@@ -62,6 +62,13 @@ struct gbsp_plan_s {
     std::vector<void*> allocs;
     char* arena = nullptr;           // one allocation carved into the plan's buffers
     size_t arena_size = 0, arena_off = 0;
+    // streaming to the host (gbsp_execute_to_host), created on first use and
+    // kept: copy stream, per-slab events, two device slabs
+    cudaStream_t stream_cs = nullptr;
+    cudaEvent_t stream_done[2] = {nullptr, nullptr}, stream_copied[2] = {nullptr, nullptr};
+    void* stream_slab[2] = {nullptr, nullptr};
+    size_t stream_slab_bytes = 0;
+    bool stream_slab_owned = false;  // allocated on first use (else carved from the arena)
 };
 
 namespace {
@@ -145,6 +152,12 @@ int allow_full_smem(F* kern) {
 void free_plan(gbsp_plan_s* p) {
     if (!p) return;
     for (void* a : p->allocs) cudaFree(a);
+    for (int b = 0; b < 2; b++) {
+        if (p->stream_slab[b] && p->stream_slab_owned) cudaFree(p->stream_slab[b]);
+        if (p->stream_done[b]) cudaEventDestroy(p->stream_done[b]);
+        if (p->stream_copied[b]) cudaEventDestroy(p->stream_copied[b]);
+    }
+    if (p->stream_cs) cudaStreamDestroy(p->stream_cs);
     delete p;
 }
 
@@ -440,6 +453,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->Lp = sp.Lp;
     p->fd = sp.ranked[0].fd;
     p->rows_threads = sp.ranked[0].nt;
+    if (o.stream_tile_rows < 0) return set_error(GBSP_ERR_INVALID, "stream_tile_rows must be >= 0");
     if (o.channel_mode < 0 || o.channel_mode > 2)
         return set_error(GBSP_ERR_INVALID, "channel_mode must be 0 (auto), 1 (clusters) or 2 (sequential)");
     // multi-channel rows run sequentially in one CTA unless clusters are asked
@@ -526,6 +540,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         }
     }
     // one device allocation for every buffer of the plan
+    const int stream_tile = (o.stream_tile_rows > 0) ? std::min(o.stream_tile_rows, p->u_tile) : 0;
+    const size_t stream_slab = (size_t)2 * stream_tile * p->out_pitch * sizeof(float2);
     {
         const int ntw_all = std::max(fft_tw_count(p->fd), 1);
         const size_t s_pitch_all = ((size_t)p->s_cols + 15) & ~(size_t)15;
@@ -538,7 +554,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
                                 (size_t)p->u_tile * s_pitch_all * sizeof(float2),
                                 (p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW)
                                     ? (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2)
-                                    : 0};
+                                    : 0,
+                                stream_slab, stream_slab};
         size_t total = 0;
         for (size_t b : sizes) total += (std::max<size_t>(b, 16) + 255) & ~(size_t)255;
         void* base = nullptr;
@@ -555,6 +572,11 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         p->arena_off = 0;
     }
     if ((rc = dev_alloc(p, (void**)&p->d_win_slot0, slot0.size()))) return rc;
+    if (stream_slab > 0) {
+        for (int b = 0; b < 2; b++)
+            if ((rc = dev_alloc(p, &p->stream_slab[b], stream_slab))) return rc;
+        p->stream_slab_bytes = stream_slab;
+    }
     if ((p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW) &&
         (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2))))
         return rc;
@@ -1219,20 +1241,6 @@ int gbsp_batch_destroy(gbsp_batch_t b) {
 // ===========================================================================
 namespace {
 
-struct StreamRes {
-    cudaStream_t cs = nullptr;
-    cudaEvent_t done[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
-    void* slab[2] = {nullptr, nullptr};
-    ~StreamRes() {
-        for (int b = 0; b < 2; b++) {
-            if (done[b]) cudaEventDestroy(done[b]);
-            if (copied[b]) cudaEventDestroy(copied[b]);
-            if (slab[b]) cudaFree(slab[b]);
-        }
-        if (cs) cudaStreamDestroy(cs);
-    }
-};
-
 }  // namespace
 
 extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch, int tile_rows, void* stream) {
@@ -1242,19 +1250,37 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
     if (tile_rows < 0) return set_error(GBSP_ERR_INVALID, "gbsp_execute_to_host: tile_rows must be >= 0");
     const int tile = std::min(tile_rows > 0 ? tile_rows : 1024, p->u_tile);
     cudaStream_t st = (cudaStream_t)stream;
-    StreamRes r;
     const size_t slab_bytes = (size_t)2 * tile * out_pitch * sizeof(float2);
-    GB_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
-    for (int b = 0; b < 2; b++) {
-        GB_CUDA(cudaEventCreateWithFlags(&r.done[b], cudaEventDisableTiming));
-        GB_CUDA(cudaEventCreateWithFlags(&r.copied[b], cudaEventDisableTiming));
-        cudaError_t e = cudaMalloc(&r.slab[b], slab_bytes);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            r.slab[b] = nullptr;
-            return set_error(GBSP_ERR_ALLOC, std::string("gbsp_execute_to_host: slab: ") + cudaGetErrorString(e));
+    if (!p->stream_cs) {
+        GB_CUDA(cudaStreamCreateWithFlags(&p->stream_cs, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; b++) {
+            GB_CUDA(cudaEventCreateWithFlags(&p->stream_done[b], cudaEventDisableTiming));
+            GB_CUDA(cudaEventCreateWithFlags(&p->stream_copied[b], cudaEventDisableTiming));
         }
     }
+    if (p->stream_slab_bytes < slab_bytes) {
+        for (int b = 0; b < 2; b++) {
+            if (p->stream_slab[b] && p->stream_slab_owned) cudaFree(p->stream_slab[b]);
+            p->stream_slab[b] = nullptr;
+        }
+        p->stream_slab_bytes = 0;
+        p->stream_slab_owned = true;
+        for (int b = 0; b < 2; b++) {
+            cudaError_t e = cudaMalloc(&p->stream_slab[b], slab_bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                p->stream_slab[b] = nullptr;
+                return set_error(GBSP_ERR_ALLOC, std::string("gbsp_execute_to_host: slab: ") + cudaGetErrorString(e));
+            }
+        }
+        p->stream_slab_bytes = slab_bytes;
+    }
+    struct {
+        cudaStream_t cs;
+        cudaEvent_t* done;
+        cudaEvent_t* copied;
+        void** slab;
+    } r{p->stream_cs, p->stream_done, p->stream_copied, p->stream_slab};
     const size_t row_bytes = out_pitch * sizeof(float2);
     char* host = static_cast<char*>(h_out);
     int rc = GBSP_OK;

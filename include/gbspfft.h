@@ -90,7 +90,9 @@ typedef struct {
                               in a thread-block cluster, 2 = one CTA runs the channels in
                               turn (results parked in an L2-resident scratch); 0 = auto
                               (2 with 512-thread row blocks, else 1)                      */
-    int reserved[1];
+    int stream_tile_rows;  /* > 0: reserve the two streaming slabs for tiles of this many
+                              Bluestein rows in the plan's own allocation
+                              (gbsp_execute_to_host then allocates nothing)               */
 } gbsp_options;
 
 typedef struct {
@@ -211,8 +213,9 @@ int gbsp_execute_noalloc(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* 
  * tile's output rows u and rows-u while the other slab is copied to h_out on
  * a second stream.  h_out: rows * out_pitch complex64 (pinned memory lets
  * the copies overlap); columns [cols/2+1, out_pitch) are written as zeros.
- * Extra device memory: 2 slabs of 2 * tile * out_pitch complex64.  Blocks
- * until the whole spectrum is in h_out. */
+ * Extra device memory: 2 slabs of 2 * tile * out_pitch complex64, kept with
+ * the plan (with a copy stream) for later calls.  Blocks until the whole
+ * spectrum is in h_out; serialise calls on one plan. */
 int gbsp_execute_to_host(gbsp_plan_t plan, void* h_out, size_t out_pitch, int tile_rows, void* stream);
 
 /* Reads and clears the plan's device error flags (synchronises the device).

@@ -97,3 +97,17 @@ def test_cli_streaming_methods(cuda, tmp_path):
     assert len(checks) == 2, res.stdout
     for ln in checks:
         assert float(ln.split("max_rel")[1].split()[0]) < 1e-4, ln
+
+
+def test_streaming_with_reserved_slabs(cuda):
+    import torch
+    coo = synthetic.uniform_matrix(1025, 777, 8000, seed=6)
+    want = streamed(coo, 256, length_policy=gb.GBSP_LEN_7SMOOTH)
+    with gb.Plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, stream_tile_rows=256) as p:
+        host = torch.zeros((coo.rows, p.output_pitch), dtype=torch.complex64).pin_memory()
+        for _ in range(2):  # the second call reuses the slabs and the copy stream
+            host.fill_(complex(9.0, 9.0))
+            p.execute_to_host(host, tile_rows=256)
+            assert np.array_equal(host.numpy(), want)
+        p.execute_to_host(host, tile_rows=1024)  # larger tiles than reserved: slabs reallocated
+        assert fp64.rel_l2(host.numpy(), want) < 1e-6
