@@ -182,13 +182,23 @@ def fft_flops_per_row(info) -> float:
     return 2 * 5.0 * L * math.log2(L) + 6.0 * L + 6.0 * (info["n_active"] + info["cols"])
 
 
-def run_batched(args, torch, gb, synthetic) -> dict:
-    """64 matrices of uneven size and sparsity: the batched form (learned
-    plans, persistent work-queue launches, one CUDA graph per pass over the
-    batch) against the plain form (one plan per matrix, analytic planner,
-    its own launches).  Outputs (3.5 GB) exceed L2, so no flush is needed."""
-    from cuspfft_gb300 import costmodel
-    mats = synthetic.batch_matrices(64)
+def small_matrices(synthetic, count: int = 256, lo: int = 100, hi: int = 1000, seed: int = 9):
+    """A batch of small matrices (dims log-uniform in [lo, hi], density
+    log-uniform in [1e-3, 3e-2]), where launch count, not arithmetic, limits
+    the one-plan-per-matrix form."""
+    import math
+    import numpy as np
+    g = np.random.default_rng(seed)
+    mats = []
+    for i in range(count):
+        r = int(math.exp(g.uniform(math.log(lo), math.log(hi))))
+        c = int(math.exp(g.uniform(math.log(lo), math.log(hi))))
+        d = float(math.exp(g.uniform(math.log(1e-3), math.log(3e-2))))
+        mats.append(synthetic.uniform_matrix(r, c, max(1, int(r * c * d)), 1000 + i))
+    return mats
+
+
+def batch_vs_plain(args, torch, gb, mats) -> tuple[float, float, object]:
     batch = gb.Batch(mats, length_policy=args.policy, planner="learned")
     outs = batch.empty_outputs()
     batch.set_outputs(outs)
@@ -214,24 +224,45 @@ def run_batched(args, torch, gb, synthetic) -> dict:
 
     ms_b = timed(batch.graph_launch)
     ms_p = timed(plain)
+    for p in plans:
+        p.close()
+    return ms_b, ms_p, batch
+
+
+def run_batched(args, torch, gb, synthetic) -> dict:
+    """64 matrices of uneven size and sparsity: the batched form (learned
+    plans, persistent work-queue launches, one CUDA graph per pass over the
+    batch) against the plain form (one plan per matrix, analytic planner,
+    its own launches).  Outputs (3.5 GB) exceed L2, so no flush is needed."""
+    from cuspfft_gb300 import costmodel
+    mats = synthetic.batch_matrices(64)
+    ms_b, ms_p, batch = batch_vs_plain(args, torch, gb, mats)
+    outs_bytes = int(sum(r * i["output_pitch"] * 8 for (r, _), i in zip(batch.shapes, batch.infos)))
     flags = batch.error_flags()
     meta = costmodel.load_model()["meta"] if costmodel.DEFAULT_MODEL.exists() else {}
-    n_sep = sum(1 for i in batch.infos if i["channels"] > 1)
+    n_sep = sum(1 for i in batch.infos if i["channels"] > 1)  # run through their own plans
     res = {
         "workload": "64 matrices, rows and cols log-uniform in [500, 12000] (half prime, half 2^a3^b5^c), "
                     "density log-uniform in [1e-4, 1e-2], seed 4",
         "unit": "matrices/s", "matrices_per_s": round(64e3 / ms_b, 1), "plain_matrices_per_s": round(64e3 / ms_p, 1),
         "speedup_vs_plain": round(ms_p / ms_b, 3), "ms_per_batch": round(ms_b, 4), "plain_ms_per_batch": round(ms_p, 4),
         "batched_form": "planner=learned, pass 1 in one work-queue launch, rows in one launch per size class, "
-                        "CUDA graph replay; cluster-split matrices through their own plans",
+                        "CUDA graph replay; multi-channel matrices through their own plans",
         "plain_form": "64 plans (analytic planner), 2 launches each",
-        "cluster_matrices": n_sep, "error_flags": flags, "steps": args.batch_steps,
-        "output_bytes": int(sum(o.numel() * 8 for o in outs)),
+        "multi_channel_matrices": n_sep, "error_flags": flags, "steps": args.batch_steps,
+        "output_bytes": outs_bytes,
         "learned_regret_heldout": meta.get("regret_learned"), "analytic_regret_heldout": meta.get("regret_analytic"),
     }
     batch.close()
-    for p in plans:
-        p.close()
+    # supplementary: small matrices, where the batched form's launch savings dominate
+    small = small_matrices(synthetic)
+    sb, sp, sbatch = batch_vs_plain(args, torch, gb, small)
+    sbatch.close()
+    res["small_matrices"] = {
+        "workload": "256 matrices, rows and cols log-uniform in [100, 1000], density log-uniform in [1e-3, 3e-2], "
+                    "seed 9 (supplementary; not the configured batched workload)",
+        "matrices_per_s": round(256e3 / sb, 1), "plain_matrices_per_s": round(256e3 / sp, 1),
+        "speedup_vs_plain": round(sp / sb, 3)}
     return res
 
 
