@@ -19,9 +19,12 @@
 
 #include "gbspfft.h"
 #include "gbsp_internal.h"
-#include "gbsp_kernels.cuh"
+#include "gbsp_launch.h"
 #include "gbsp_planner.h"
+#include "gbsp_tables.cuh"
 
+using gbsp::DeviceLimits;
+using gbsp::device_limits;
 using gbsp::set_error;
 using gbsp::rows_smem_bytes;
 using gbsp::fft_tw_count;
@@ -73,14 +76,6 @@ struct gbsp_plan_s {
 
 namespace {
 
-#define GB_CUDA(call)                                                                     \
-    do {                                                                                  \
-        cudaError_t e_ = (call);                                                          \
-        if (e_ != cudaSuccess)                                                            \
-            return set_error(e_ == cudaErrorMemoryAllocation ? GBSP_ERR_ALLOC : GBSP_ERR_CUDA, \
-                             std::string(#call) + ": " + cudaGetErrorString(e_));        \
-    } while (0)
-
 // Carves `bytes` (256-byte aligned) from the plan's arena when it has room,
 // else allocates on its own.
 int dev_alloc(gbsp_plan_s* p, void** ptr, size_t bytes) {
@@ -102,53 +97,6 @@ int dev_alloc(gbsp_plan_s* p, void** ptr, size_t bytes) {
     return GBSP_OK;
 }
 
-// Per-device limits the planner needs, queried once per device (a full
-// cudaGetDeviceProperties costs far more than the two attributes).
-struct DeviceLimits {
-    size_t smem_optin = 0;
-    int sms = 0;
-};
-int device_limits(int dev, DeviceLimits* out) {
-    constexpr int kMaxDev = 64;
-    static std::mutex mu;
-    static DeviceLimits cache[kMaxDev];
-    if (dev < 0 || dev >= kMaxDev) return set_error(GBSP_ERR_UNSUPPORTED, "device index out of range");
-    std::lock_guard<std::mutex> lk(mu);
-    if (cache[dev].sms == 0) {
-        int optin = 0, sms = 0;
-        GB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        cache[dev].smem_optin = (size_t)optin;
-        cache[dev].sms = sms;
-    }
-    *out = cache[dev];
-    return GBSP_OK;
-}
-
-// Lets `kern` take all the opt-in shared memory of a CTA.  The limit is a
-// property of the kernel, shared by every plan in the process; one fixed
-// value keeps a later, smaller plan from invalidating an earlier one.  Done
-// once per (kernel, device).
-std::mutex g_smem_mu;
-std::vector<std::pair<const void*, int>> g_smem_done;  // (kernel, device) already raised
-
-template <typename F>
-int allow_full_smem(F* kern) {
-    int dev = 0;
-    GB_CUDA(cudaGetDevice(&dev));
-    const std::pair<const void*, int> key((const void*)kern, dev);
-    std::lock_guard<std::mutex> lk(g_smem_mu);
-    if (std::find(g_smem_done.begin(), g_smem_done.end(), key) != g_smem_done.end()) return GBSP_OK;
-    cudaFuncAttributes fa;
-    DeviceLimits lim;
-    GB_CUDA(cudaFuncGetAttributes(&fa, kern));
-    if (int rc = device_limits(dev, &lim)) return rc;
-    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)lim.smem_optin - (int)fa.sharedSizeBytes));
-    g_smem_done.push_back(key);
-    return GBSP_OK;
-}
-
 void free_plan(gbsp_plan_s* p) {
     if (!p) return;
     for (void* a : p->allocs) cudaFree(a);
@@ -163,12 +111,14 @@ void free_plan(gbsp_plan_s* p) {
 
 inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-template <typename IDX, int TAB, bool BIG, int KU>
+gbsp::P1Kernel p1_kernel(const gbsp_plan_s* p) {
+    return gbsp::P1Kernel{p->idx_bytes, p->tab_mode, p->big != 0, p->p1_ku};
+}
+
+// sizes pass 1's persistent grid (and raises the kernel's shared-memory limit)
 int p1_prepare(gbsp_plan_s* p, int sms) {
-    auto kern = gbsp::k_twiddle_sum<IDX, TAB, BIG, KU>;
-    if (int rc = allow_full_smem(kern)) return rc;
     int nb = 0;
-    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, gbsp::P1_THREADS, p->p1_smem));
+    if (int rc = gbsp::p1_blocks_per_sm(p1_kernel(p), p->p1_smem, &nb)) return rc;
     if (nb < 1) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 kernel does not fit on an SM");
     p->p1_grid = nb * sms;
     return GBSP_OK;
@@ -197,96 +147,14 @@ gbsp::P1Args p1_args(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pi
     return a;
 }
 
-template <typename IDX, int TAB, bool BIG, int KU>
-void p1_launch(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pitch, const float2* chirp,
-               cudaStream_t st) {
-    gbsp::k_twiddle_sum<IDX, TAB, BIG, KU><<<p->p1_grid, gbsp::P1_THREADS, p->p1_smem, st>>>(
-        p1_args(p, u0, n, S, s_pitch, chirp));
-}
-
-// prepare == true: set attributes and grid; false: launch
-template <typename IDX, int TAB, bool BIG>
-int p1_dispatch_ku(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
-                   const float2* chirp, cudaStream_t st) {
-    if (p->p1_ku == 8) {
-        if (prepare) return p1_prepare<IDX, TAB, BIG, 8>(p, sms);
-        p1_launch<IDX, TAB, BIG, 8>(p, u0, n, S, sp, chirp, st);
-    } else {
-        if (prepare) return p1_prepare<IDX, TAB, BIG, 4>(p, sms);
-        p1_launch<IDX, TAB, BIG, 4>(p, u0, n, S, sp, chirp, st);
-    }
-    return GBSP_OK;
-}
-
-// 16-bit indices only occur with rows <= 65536 (no 64-bit phase products)
-template <int TAB>
-int p1_dispatch_tab(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
-                    const float2* chirp, cudaStream_t st) {
-    if (p->idx_bytes == 2) return p1_dispatch_ku<uint16_t, TAB, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
-    if (p->big) return p1_dispatch_ku<uint32_t, TAB, true>(p, prepare, sms, u0, n, S, sp, chirp, st);
-    return p1_dispatch_ku<uint32_t, TAB, false>(p, prepare, sms, u0, n, S, sp, chirp, st);
-}
-
-int p1_dispatch(gbsp_plan_s* p, bool prepare, int sms, int u0, int n, float2* S, size_t sp,
-                const float2* chirp, cudaStream_t st) {
-    switch (p->tab_mode) {
-        case gbsp::TAB_HALF: return p1_dispatch_tab<gbsp::TAB_HALF>(p, prepare, sms, u0, n, S, sp, chirp, st);
-        case gbsp::TAB_TWO: return p1_dispatch_tab<gbsp::TAB_TWO>(p, prepare, sms, u0, n, S, sp, chirp, st);
-        default: return p1_dispatch_tab<gbsp::TAB_FULL>(p, prepare, sms, u0, n, S, sp, chirp, st);
-    }
-}
-
 // chirp == nullptr gives the raw column sums (gbsp_column_sums)
 int launch_pass1(const gbsp_plan_s* p, int u0, int n, float2* S, size_t sp, const float2* chirp,
                  cudaStream_t st) {
-    p1_dispatch(const_cast<gbsp_plan_s*>(p), false, 0, u0, n, S, sp, chirp, st);
-    GB_CUDA(cudaGetLastError());
-    return GBSP_OK;
+    return gbsp::p1_launch(p1_kernel(p), p->p1_grid, p->p1_smem, st, p1_args(p, u0, n, S, sp, chirp));
 }
 
-// Launch configuration of the row kernel: a plain grid for one channel, a
-// cluster of K CTAs per row otherwise.  NTMAX is the compiled block-size
-// bound (1024: 64 registers a thread; 512: 128, for radices above 16); the
-// block itself has p->rows_threads threads.
-template <int MODE>
-cudaLaunchConfig_t rows_config(const gbsp_plan_s* p, unsigned grid, unsigned nt, cudaStream_t st,
-                               cudaLaunchAttribute* attr) {
-    constexpr bool CL = MODE == gbsp::ROW_CLUSTER;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(nt);
-    cfg.dynamicSmemBytes = p->rows_smem;
-    cfg.stream = st;
-    if (CL) {
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = p->K;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-    }
-    return cfg;
-}
-
-// Sets the kernel's shared-memory limit and returns how many CTAs (single
-// channel, sequential channels) or clusters of p->rows_threads threads can be
-// resident at once.
-template <int MODE, int NTMAX>
-int rows_capacity(const gbsp_plan_s* p, int sms, int* cap) {
-    constexpr bool CL = MODE == gbsp::ROW_CLUSTER;
-    auto kern = gbsp::k_bluestein_rows<NTMAX, MODE>;
-    if (int rc = allow_full_smem(kern)) return rc;
-    *cap = 0;
-    if (!CL) {
-        int nb = 0;
-        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, p->rows_threads, p->rows_smem));
-        *cap = nb * sms;
-    } else {
-        cudaLaunchAttribute attr[1];
-        cudaLaunchConfig_t cfg = rows_config<MODE>(p, (unsigned)(p->K * sms), p->rows_threads, nullptr, attr);
-        GB_CUDA(cudaOccupancyMaxActiveClusters(cap, kern, &cfg));
-    }
-    return GBSP_OK;
+gbsp::RowsKernel rows_kernel(const gbsp_plan_s* p) {
+    return gbsp::RowsKernel{p->row_mode, p->rows_ntmax, p->K, p->rows_threads, p->rows_smem};
 }
 
 gbsp::RowsArgs rows_args(const gbsp_plan_s* p, const float2* S, size_t s_pitch, int u0, int n, void* d_out,
@@ -314,29 +182,8 @@ gbsp::RowsArgs rows_args(const gbsp_plan_s* p, const float2* S, size_t s_pitch, 
 
 // the row kernel with fully specified arguments (input tile, output slab
 // and row map)
-template <int MODE, int NTMAX>
-int rows_launch_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
-    cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = rows_config<MODE>(p, (unsigned)p->rows_grid, p->rows_threads, st, attr);
-    GB_CUDA(cudaLaunchKernelEx(&cfg, gbsp::k_bluestein_rows<NTMAX, MODE>, a, p->fd, p->d_err));
-    return GBSP_OK;
-}
-
-// Instances: single channel and clusters with both block-size bounds,
-// sequential channels with the 512-thread bound.
 int launch_rows_args(const gbsp_plan_s* p, const gbsp::RowsArgs& a, cudaStream_t st) {
-    using namespace gbsp;
-    const bool n512 = p->rows_ntmax == 512;
-    switch (p->row_mode) {
-        case ROW_SINGLE:
-            return n512 ? rows_launch_args<ROW_SINGLE, 512>(p, a, st) : rows_launch_args<ROW_SINGLE, 1024>(p, a, st);
-        case ROW_CLUSTER:
-            return n512 ? rows_launch_args<ROW_CLUSTER, 512>(p, a, st) : rows_launch_args<ROW_CLUSTER, 1024>(p, a, st);
-        case ROW_SEQ:
-            return rows_launch_args<ROW_SEQ, 512>(p, a, st);
-        default:
-            return rows_launch_args<ROW_SEQW, 512>(p, a, st);
-    }
+    return gbsp::rows_launch(rows_kernel(p), p->rows_grid, st, a, p->fd, p->d_err);
 }
 
 int launch_rows(const gbsp_plan_s* p, int u0, int n, void* d_out, size_t out_pitch, cudaStream_t st) {
@@ -359,21 +206,8 @@ int rows_prepare(gbsp_plan_s* p, int sms) {
         return set_error(GBSP_ERR_UNSUPPORTED, "more than " + std::to_string(MAX_CHANNELS) +
                                                    " channels need sequential channels (512-thread rows)");
     if (p->row_mode == ROW_SEQ && p->K > MAX_CHANNELS) p->row_mode = ROW_SEQW;
-    int cap = 0, rc;
-    const bool n512 = p->rows_ntmax == 512;
-    switch (p->row_mode) {
-        case ROW_SINGLE:
-            rc = n512 ? rows_capacity<ROW_SINGLE, 512>(p, sms, &cap) : rows_capacity<ROW_SINGLE, 1024>(p, sms, &cap);
-            break;
-        case ROW_CLUSTER:
-            rc = n512 ? rows_capacity<ROW_CLUSTER, 512>(p, sms, &cap) : rows_capacity<ROW_CLUSTER, 1024>(p, sms, &cap);
-            break;
-        case ROW_SEQ:
-            rc = rows_capacity<ROW_SEQ, 512>(p, sms, &cap);
-            break;
-        default:
-            rc = rows_capacity<ROW_SEQW, 512>(p, sms, &cap);
-    }
+    int cap = 0;
+    const int rc = rows_capacity(rows_kernel(p), sms, &cap);
     if (rc) return rc;
     if (cap < 1) return set_error(GBSP_ERR_UNSUPPORTED, "row kernel does not fit on an SM");
     p->rows_grid = (p->row_mode == ROW_CLUSTER) ? cap * p->K : cap;
@@ -494,7 +328,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         p->ntab = (int)gbsp::row_table_entries(sh.tab, p->rows);
         p->p1_smem = gbsp::p1_smem_bytes(sh, p->rows);
     }
-    if ((rc = p1_dispatch(p, true, sms, 0, 0, nullptr, 0, nullptr, st))) return rc;
+    if ((rc = p1_prepare(p, sms))) return rc;
 
     // ---- row-kernel configuration
     p->rows_smem = rows_smem_bytes(p->fd);
@@ -928,41 +762,18 @@ int batch_alloc(gbsp_batch_s* b, void** ptr, size_t bytes) {
     return GBSP_OK;
 }
 
-template <typename IDX, int TAB, bool BIG, int KU>
-int p1b_run(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    auto kern = gbsp::k_twiddle_sum_batch<IDX, TAB, BIG, KU>;
+// prepare: size the batched pass-1 grid; else launch it
+int p1b_dispatch(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
+    const gbsp::P1Kernel k{b->idx_bytes, b->tab, b->big != 0, b->ku};
     if (prepare) {
-        if (int rc = allow_full_smem(kern)) return rc;
         int nb = 0;
-        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, gbsp::P1_THREADS, b->p1_smem));
+        if (int rc = gbsp::p1_batch_blocks_per_sm(k, b->p1_smem, &nb)) return rc;
         if (nb < 1) return set_error(GBSP_ERR_UNSUPPORTED, "batched pass 1 does not fit on an SM");
         b->p1_grid = nb * sms;
         return GBSP_OK;
     }
-    kern<<<b->p1_grid, gbsp::P1_THREADS, b->p1_smem, st>>>(b->d_p1, b->d_p1_begin, (int)b->order.size(),
-                                                            b->d_queue);
-    GB_CUDA(cudaGetLastError());
-    return GBSP_OK;
-}
-
-template <typename IDX, int TAB, bool BIG>
-int p1b_ku(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    return b->ku == 8 ? p1b_run<IDX, TAB, BIG, 8>(b, prepare, sms, st) : p1b_run<IDX, TAB, BIG, 4>(b, prepare, sms, st);
-}
-
-template <int TAB>
-int p1b_tab(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    if (b->idx_bytes == 2) return p1b_ku<uint16_t, TAB, false>(b, prepare, sms, st);
-    if (b->big) return p1b_ku<uint32_t, TAB, true>(b, prepare, sms, st);
-    return p1b_ku<uint32_t, TAB, false>(b, prepare, sms, st);
-}
-
-int p1b_dispatch(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    switch (b->tab) {
-        case gbsp::TAB_HALF: return p1b_tab<gbsp::TAB_HALF>(b, prepare, sms, st);
-        case gbsp::TAB_TWO: return p1b_tab<gbsp::TAB_TWO>(b, prepare, sms, st);
-        default: return p1b_tab<gbsp::TAB_FULL>(b, prepare, sms, st);
-    }
+    return gbsp::p1_batch_launch(k, b->p1_grid, b->p1_smem, st, b->d_p1, b->d_p1_begin, (int)b->order.size(),
+                                 b->d_queue);
 }
 
 int batch_launch(gbsp_batch_s* b, cudaStream_t st) {
@@ -972,9 +783,10 @@ int batch_launch(gbsp_batch_s* b, cudaStream_t st) {
         if (rc) return rc;
         for (size_t c = 0; c < b->classes.size(); c++) {
             const auto& k = b->classes[c];
-            gbsp::k_bluestein_rows_batch<512><<<k.grid, k.nt, k.smem, st>>>(
-                b->d_rows + k.begin, b->d_row_begin + k.begin + c, k.end - k.begin, b->d_queue + 1 + c, b->d_err);
-            GB_CUDA(cudaGetLastError());
+            if ((rc = gbsp::rows_batch_launch(k.grid, k.nt, k.smem, st, b->d_rows + k.begin,
+                                              b->d_row_begin + k.begin + c, k.end - k.begin, b->d_queue + 1 + c,
+                                              b->d_err)))
+                return rc;
         }
     }
     for (int m : b->separate) {
@@ -1062,11 +874,6 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
     // Single-channel matrices go through the queues, grouped into classes of
     // (block size, CTAs per SM), classes with the longest rows first, and by
     // decreasing channel length inside a class.
-    auto kern = gbsp::k_bluestein_rows_batch<512>;
-    if ((rc = allow_full_smem(kern))) {
-        free_batch(b);
-        return rc;
-    }
     std::vector<int> per_sm(count, 0);
     for (int i = 0; i < count; i++) {
         const gbsp_plan_s* p = b->plans[i];
@@ -1074,8 +881,7 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
             b->separate.push_back(i);
             continue;
         }
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[i], kern, p->rows_threads,
-                                                          rows_smem_bytes(p->fd)) != cudaSuccess ||
+        if (gbsp::rows_batch_blocks_per_sm(p->rows_threads, rows_smem_bytes(p->fd), &per_sm[i]) != GBSP_OK ||
             per_sm[i] < 1) {
             free_batch(b);
             return set_error(GBSP_ERR_UNSUPPORTED, "gbsp_batch_create: batched row kernel does not fit");

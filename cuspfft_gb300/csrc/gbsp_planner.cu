@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -11,6 +12,7 @@
 
 #include "gbsp_fft.cuh"
 #include "gbsp_internal.h"
+#include "gbsp_launch.h"
 #include "gbsp_planner.h"
 
 namespace gbsp {
@@ -207,6 +209,41 @@ std::vector<int> fitting_p1_shapes(int rows, size_t smem_cap, int table_mode) {
         if (table_mode != 0) break;
     }
     return out;
+}
+
+int device_limits(int dev, DeviceLimits* out) {
+    constexpr int kMaxDev = 64;
+    static std::mutex mu;
+    static DeviceLimits cache[kMaxDev];
+    if (dev < 0 || dev >= kMaxDev) return set_error(GBSP_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (cache[dev].sms == 0) {
+        int optin = 0, sms = 0;
+        GB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cache[dev].smem_optin = (size_t)optin;
+        cache[dev].sms = sms;
+    }
+    *out = cache[dev];
+    return GBSP_OK;
+}
+
+int allow_full_smem(const void* kern) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void*, int>> done;  // (kernel, device) already raised
+    int dev = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    const std::pair<const void*, int> key(kern, dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), key) != done.end()) return GBSP_OK;
+    cudaFuncAttributes fa;
+    DeviceLimits lim;
+    GB_CUDA(cudaFuncGetAttributes(&fa, kern));
+    if (int rc = device_limits(dev, &lim)) return rc;
+    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)lim.smem_optin - (int)fa.sharedSizeBytes));
+    done.push_back(key);
+    return GBSP_OK;
 }
 
 size_t device_smem_cap() {
