@@ -165,7 +165,7 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
         float2 blk[KU];
 #pragma unroll
         for (int i = 0; i < KU; i++) blk[i] = make_float2(0.f, 0.f);
-#pragma unroll 2
+#pragma unroll 4
         for (int i = 0; i < cnt; i++) {
             const NzInfo z = info[i];  // one broadcast 16-byte load
             const float2 wd = make_float2(z.wx, z.wy);
