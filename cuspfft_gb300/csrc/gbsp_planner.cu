@@ -425,8 +425,10 @@ int gbsp_autotune(int rows, int cols, int n_active, int nnz, const int* col_ptr,
         }
         gbsp_plan_destroy(pl);
     }
-    cudaFree(d_out);
-    if (rc) return rc;
+    if (rc) {
+        cudaFree(d_out);
+        return rc;
+    }
     int bi = 0, bj = 0;
     for (int i = 0; i < nr; i++)
         for (int j = 0; j < np; j++) {
@@ -442,7 +444,39 @@ int gbsp_autotune(int rows, int cols, int n_active, int nnz, const int* col_ptr,
             }
         }
     *best = c[(size_t)bi * np + bj];
-    return GBSP_OK;
+    // The --csc-tile analogue: Bluestein rows per tile, at most the caller's
+    // u_tile (0 = all rows); smaller tiles bound the scratch memory, and the
+    // fastest of {limit, limit/2, limit/4} is kept.
+    {
+        const int half_rows = rows / 2 + 1;
+        const int limit = (b.u_tile > 0) ? std::min(b.u_tile, half_rows) : half_rows;
+        float best_ms = INFINITY;
+        int best_tile = limit;
+        for (int div = 1; div <= 4 && rc == GBSP_OK; div *= 2) {
+            const int tile = std::max(1, limit / div);
+            if (div > 1 && tile == limit / (div / 2)) break;
+            gbsp_options o = *best;
+            o.u_tile = tile;
+            gbsp_plan_t pl = nullptr;
+            if ((rc = gbsp_plan_create(rows, cols, n_active, nnz, col_ptr, row_idx, sparse_cols, &o, stream, &pl)))
+                break;
+            rc = gbsp_execute(pl, d_out, pitch, stream);
+            float tot = INFINITY;
+            for (int r = 0; r < reps && rc == GBSP_OK; r++) {
+                float x = 0.f, y = 0.f;
+                rc = gbsp_execute_profiled(pl, d_out, pitch, stream, &x, &y);
+                tot = std::min(tot, x + y);
+            }
+            gbsp_plan_destroy(pl);
+            if (tot < best_ms) {
+                best_ms = tot;
+                best_tile = tile;
+            }
+        }
+        if (rc == GBSP_OK) best->u_tile = (best_tile == half_rows) ? 0 : best_tile;
+    }
+    cudaFree(d_out);
+    return rc;
 }
 
 }  // extern "C"

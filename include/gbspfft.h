@@ -297,7 +297,10 @@ typedef struct {
  * buffer allocated for the duration).  Pass 1 depends only on the pass-1
  * shape and the rows only on the row choice, so max(n_rows, n_p1) plans
  * cover the whole cross product; entries[i * n_p1 + j] holds the composed
- * times.  *best receives the candidate with the least total.  Blocking. */
+ * times.  *best receives the candidate with the least total, with u_tile
+ * (the --csc-tile analogue) chosen last among {cap, cap/2, cap/4} where cap
+ * is base->u_tile (0 = all rows; smaller tiles bound the scratch memory).
+ * Blocking. */
 int gbsp_autotune(int rows, int cols, int n_active, int nnz, const int* col_ptr, const int* row_idx,
                   const int* sparse_cols, const gbsp_options* base, int max_rows_cands, int reps,
                   void* stream, gbsp_options* best, gbsp_tune_entry* entries, int cap,

@@ -89,6 +89,8 @@ def test_autotune_small_matrix(cuda):
     i, j = np.unravel_index(np.argmin(tot), tot.shape)
     assert tr.best.radices() == tr.candidates[i * tr.n_p1 + j].radices()
     assert tr.best.pass1_shape == tr.candidates[i * tr.n_p1 + j].pass1_shape
+    half = coo.rows // 2 + 1
+    assert tr.best.u_tile in (0, half // 2, half // 4)
     with gb.Plan(coo, options=tr.best) as plan:
         out = plan.empty_output()
         plan.execute(out)
@@ -97,6 +99,13 @@ def test_autotune_small_matrix(cuda):
         got = out.cpu().numpy()[:, :coo.cols // 2 + 1]
     ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx)
     assert fp64.rel_l2(got, ref) < 1e-5
+
+
+def test_autotune_tile_respects_the_callers_limit(cuda):
+    coo = synthetic.uniform_matrix(601, 900, 6000, seed=8)
+    tr = tuning.autotune(coo, reps=1, max_rows_cands=2, u_tile=128)
+    assert tr.best.u_tile in (128, 64, 32)
+    assert all(c.u_tile == 128 for c in tr.candidates)
 
 
 def test_learned_planner_picks_the_predicted_best(cuda):
