@@ -24,6 +24,7 @@ GBSP_LEN_3SMOOTH = 3
 GBSP_LEN_7SMOOTH = 7
 GBSP_PLANNER_MODEL = 0
 GBSP_PLANNER_LEARNED = 1
+GBSP_STREAM_TILE_AUTO = -1  # GbspOptions.stream_tile_rows: slabs for the automatic tile
 GBSP_N_PASS1_SHAPES = 8
 GBSP_N_FEATURES = 36
 GBSP_MLP_HIDDEN = 64

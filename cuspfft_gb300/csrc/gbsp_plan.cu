@@ -71,6 +71,7 @@ struct gbsp_plan_s {
     cudaEvent_t stream_done[2] = {nullptr, nullptr}, stream_copied[2] = {nullptr, nullptr};
     void* stream_slab[2] = {nullptr, nullptr};
     size_t stream_slab_bytes = 0;
+    int stream_tile_auto = 1;        // tile_rows 0 of gbsp_execute_to_host
     bool stream_slab_owned = false;  // allocated on first use (else carved from the arena)
 };
 
@@ -228,9 +229,7 @@ int validate_csc(int rows, int cols, int n_active, int nnz, const int* col_ptr,
         if (sparse_cols[j] < 0 || sparse_cols[j] >= cols || (j > 0 && sparse_cols[j] <= sparse_cols[j - 1]))
             return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: sparse_cols not strictly increasing in [0,cols)");
     }
-    for (int i = 0; i < nnz; i++)
-        if (row_idx[i] < 0 || row_idx[i] >= rows)
-            return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: row index out of range");
+    // row indices are checked on the device while they are uploaded (plan_build)
     return GBSP_OK;
 }
 
@@ -287,7 +286,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->Lp = sp.Lp;
     p->fd = sp.ranked[0].fd;
     p->rows_threads = sp.ranked[0].nt;
-    if (o.stream_tile_rows < 0) return set_error(GBSP_ERR_INVALID, "stream_tile_rows must be >= 0");
+    if (o.stream_tile_rows < GBSP_STREAM_TILE_AUTO)
+        return set_error(GBSP_ERR_INVALID, "stream_tile_rows must be >= 0 or GBSP_STREAM_TILE_AUTO");
     if (o.channel_mode < 0 || o.channel_mode > 2)
         return set_error(GBSP_ERR_INVALID, "channel_mode must be 0 (auto), 1 (clusters) or 2 (sequential)");
     // multi-channel rows run sequentially in one CTA unless clusters are asked
@@ -334,8 +334,10 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->rows_smem = rows_smem_bytes(p->fd);
     if ((rc = rows_prepare(p, sms))) return rc;
 
-    // ---- CSC upload (rows in column order) and the pass-1 task tables: each
-    // window's nonzeros cut into at most cw + P1_WARPS balanced tasks
+    // ---- pass-1 task tables: each window's nonzeros cut into at most
+    // cw + P1_WARPS balanced tasks, longest first.  Built in one host buffer
+    // laid out like its device copy (slot0 | task | task_col), so one copy
+    // uploads it.
     const int na = p->n_active;
     std::vector<int> colp(p->cols + 1, 0);
     for (int j = 0; j < na; j++) colp[sparse_cols[j] + 1] = col_ptr[j + 1] - col_ptr[j];
@@ -343,9 +345,16 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->s_cols = (p->cols + 1) & ~1;
     const int CW = p->p1_cw, VM = gbsp::p1_vmax(p->p1_cw);
     const int n_win = (p->s_cols + CW - 1) / CW;
-    std::vector<uint8_t> slot0((size_t)n_win * (CW + 1));
-    std::vector<int2> task((size_t)n_win * VM, make_int2(0, 0));
-    std::vector<uint8_t> task_col((size_t)n_win * VM, 0);
+    const size_t n_slot = (size_t)n_win * (CW + 1), n_task = (size_t)n_win * VM;
+    const size_t off_task = (n_slot + 15) & ~(size_t)15;
+    const size_t off_col = off_task + n_task * sizeof(int2);
+    const size_t tbl_bytes = off_col + n_task;
+    std::vector<uint8_t> tbl(tbl_bytes, 0);
+    uint8_t* slot0 = tbl.data();
+    int2* task = reinterpret_cast<int2*>(tbl.data() + off_task);
+    uint8_t* task_col = tbl.data() + off_col;
+    struct Task { int b, e, col; };
+    std::vector<Task> ts(VM);
     for (int w = 0; w < n_win; w++) {
         auto deg = [&](int lc) {
             const int c = w * CW + lc;
@@ -354,38 +363,52 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         long sum = 0;
         for (int lc = 0; lc < CW; lc++) sum += deg(lc);
         const long T = std::max<long>(32, (sum + gbsp::P1_WARPS - 1) / gbsp::P1_WARPS);
-        struct Task { int b, e, col; };
-        std::vector<Task> ts;
+        int nt = 0;
         for (int lc = 0; lc < CW; lc++) {
-            slot0[(size_t)w * (CW + 1) + lc] = (uint8_t)ts.size();
+            slot0[(size_t)w * (CW + 1) + lc] = (uint8_t)nt;
             const int d = deg(lc);
             if (d == 0) continue;
             const int np = (int)((d + T - 1) / T);
+            if (nt + np > VM) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 window task overflow");
             const int base = colp[w * CW + lc];
-            for (int k = 0; k < np; k++)
-                ts.push_back({base + (int)((long)k * d / np), base + (int)((long)(k + 1) * d / np), (int)ts.size()});
+            for (int k = 0; k < np; k++, nt++)
+                ts[nt] = {base + (int)((long)k * d / np), base + (int)((long)(k + 1) * d / np), nt};
         }
-        if ((int)ts.size() > VM) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 window task overflow");
-        slot0[(size_t)w * (CW + 1) + CW] = (uint8_t)ts.size();
-        std::stable_sort(ts.begin(), ts.end(), [](const Task& a, const Task& b) { return a.e - a.b > b.e - b.b; });
-        for (size_t i = 0; i < ts.size(); i++) {
+        slot0[(size_t)w * (CW + 1) + CW] = (uint8_t)nt;
+        // longest first, ties in creation order
+        std::sort(ts.begin(), ts.begin() + nt, [](const Task& a, const Task& b) {
+            const int la = a.e - a.b, lb = b.e - b.b;
+            return la != lb ? la > lb : a.col < b.col;
+        });
+        for (int i = 0; i < nt; i++) {
             task[(size_t)w * VM + i] = make_int2(ts[i].b, ts[i].e);
             task_col[(size_t)w * VM + i] = (uint8_t)ts[i].col;
         }
     }
     // one device allocation for every buffer of the plan
-    const int stream_tile = (o.stream_tile_rows > 0) ? std::min(o.stream_tile_rows, p->u_tile) : 0;
+    {
+        // automatic streaming tile: ~half_rows / 9, to the nearest multiple
+        // of the SM count (at least one), at most u_tile
+        const int t = (p->half_rows + 8) / 9;
+        p->stream_tile_auto = std::min(p->u_tile, std::max(sms, (t + sms / 2) / sms * sms));
+    }
+    const int stream_tile = (o.stream_tile_rows > 0)                       ? std::min(o.stream_tile_rows, p->u_tile)
+                            : (o.stream_tile_rows == GBSP_STREAM_TILE_AUTO) ? p->stream_tile_auto
+                                                                            : 0;
     const size_t stream_slab = (size_t)2 * stream_tile * p->out_pitch * sizeof(float2);
+    p->s_pitch = ((size_t)p->s_cols + 15) & ~(size_t)15;  // 128-byte rows; the bulk copy needs 16
+    const size_t s_bytes = (size_t)p->u_tile * p->s_pitch * sizeof(float2);
+    // u16 indices are narrowed on the device from an int32 copy staged in the
+    // S tile, or in a region of their own when the tile is smaller
+    const size_t idx_in_bytes = (size_t)p->nnz * sizeof(int);
+    const size_t staging = (p->idx_bytes == 2 && idx_in_bytes > s_bytes) ? idx_in_bytes : 0;
     {
         const int ntw_all = std::max(fft_tw_count(p->fd), 1);
-        const size_t s_pitch_all = ((size_t)p->s_cols + 15) & ~(size_t)15;
-        const size_t sizes[] = {slot0.size(), task.size() * sizeof(int2), task_col.size(),
-                                (size_t)std::max(p->nnz, 1) * p->idx_bytes, sizeof(int),
+        const size_t sizes[] = {tbl_bytes, (size_t)std::max(p->nnz, 1) * p->idx_bytes, 2 * sizeof(int),
                                 (size_t)p->ntab * sizeof(float2), (size_t)p->K * p->cols * sizeof(float2),
                                 (size_t)p->K * p->cols * sizeof(float2), (size_t)p->K * p->Lp * sizeof(float2),
                                 (size_t)ntw_all * sizeof(float2), (size_t)p->K * p->Lp * sizeof(double2),
-                                (size_t)p->K * p->Lp * sizeof(double2),
-                                (size_t)p->u_tile * s_pitch_all * sizeof(float2),
+                                (size_t)p->K * p->Lp * sizeof(double2), s_bytes, staging,
                                 (p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW)
                                     ? (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2)
                                     : 0,
@@ -405,7 +428,11 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         p->arena_size = total;
         p->arena_off = 0;
     }
-    if ((rc = dev_alloc(p, (void**)&p->d_win_slot0, slot0.size()))) return rc;
+    uint8_t* d_tbl = nullptr;
+    if ((rc = dev_alloc(p, (void**)&d_tbl, tbl_bytes))) return rc;
+    p->d_win_slot0 = d_tbl;
+    p->d_win_task = reinterpret_cast<int2*>(d_tbl + off_task);
+    p->d_win_task_col = d_tbl + off_col;
     if (stream_slab > 0) {
         for (int b = 0; b < 2; b++)
             if ((rc = dev_alloc(p, &p->stream_slab[b], stream_slab))) return rc;
@@ -414,25 +441,22 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     if ((p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW) &&
         (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2))))
         return rc;
-    if ((rc = dev_alloc(p, (void**)&p->d_win_task, task.size() * sizeof(int2)))) return rc;
-    if ((rc = dev_alloc(p, (void**)&p->d_win_task_col, task_col.size()))) return rc;
     if ((rc = dev_alloc(p, &p->d_row_idx, (size_t)std::max(p->nnz, 1) * p->idx_bytes))) return rc;
-    if ((rc = dev_alloc(p, (void**)&p->d_err, sizeof(int)))) return rc;
-    GB_CUDA(cudaMemsetAsync(p->d_err, 0, sizeof(int), st));
-    GB_CUDA(cudaMemcpyAsync(p->d_win_slot0, slot0.data(), slot0.size(), cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(p->d_win_task, task.data(), task.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(p->d_win_task_col, task_col.data(), task_col.size(), cudaMemcpyHostToDevice, st));
-    std::vector<uint16_t> r16;
+    if ((rc = dev_alloc(p, (void**)&p->d_err, 2 * sizeof(int)))) return rc;  // [1]: bad row index
+    if ((rc = dev_alloc(p, (void**)&p->d_S, s_bytes))) return rc;
+    GB_CUDA(cudaMemsetAsync(p->d_err, 0, 2 * sizeof(int), st));
+    GB_CUDA(cudaMemcpyAsync(d_tbl, tbl.data(), tbl_bytes, cudaMemcpyHostToDevice, st));
     if (p->nnz > 0) {
+        int* d_in = static_cast<int*>(p->d_row_idx);
         if (p->idx_bytes == 2) {
-            r16.resize(p->nnz);
-            for (int i = 0; i < p->nnz; i++) r16[i] = (uint16_t)row_idx[i];
-            GB_CUDA(cudaMemcpyAsync(p->d_row_idx, r16.data(), (size_t)p->nnz * 2,
-                                    cudaMemcpyHostToDevice, st));
-        } else {
-            GB_CUDA(cudaMemcpyAsync(p->d_row_idx, row_idx, (size_t)p->nnz * 4,
-                                    cudaMemcpyHostToDevice, st));
+            d_in = reinterpret_cast<int*>(p->d_S);
+            if (staging > 0 && (rc = dev_alloc(p, (void**)&d_in, staging))) return rc;
         }
+        GB_CUDA(cudaMemcpyAsync(d_in, row_idx, idx_in_bytes, cudaMemcpyHostToDevice, st));
+        gbsp::k_row_index_in<<<(int)std::min<long>(blocks_for(p->nnz, 256), (long)sms * 8), 256, 0, st>>>(
+            d_in, p->idx_bytes == 2 ? static_cast<uint16_t*>(p->d_row_idx) : nullptr, p->nnz, p->rows,
+            p->d_err + 1);
+        GB_CUDA(cudaGetLastError());
     }
 
     // ---- tables (FP64 on the device, rounded to FP32)
@@ -476,14 +500,12 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
             p->d_filt, d_spec[cur], K, Lp, p->fd.R[p->fd.nst - 1], 1.0 / (double)p->L);
         e = cudaGetLastError();
     }
+    int bad_row = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad_row, p->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return set_error(GBSP_ERR_CUDA, std::string("plan tables: ") + cudaGetErrorString(e));
-
-    // ---- pass-1 scratch tile
-    // rows start on 128-byte boundaries; the bulk copy needs 16
-    p->s_pitch = ((size_t)p->s_cols + 15) & ~(size_t)15;
-    if ((rc = dev_alloc(p, (void**)&p->d_S, (size_t)p->u_tile * p->s_pitch * sizeof(float2)))) return rc;
+    if (bad_row) return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: row index out of range");
     return GBSP_OK;
 }
 
@@ -1054,7 +1076,7 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
     if (out_pitch < (size_t)p->out_cols || (out_pitch & 1))
         return set_error(GBSP_ERR_INVALID, "gbsp_execute_to_host: out_pitch must be even and >= cols/2+1");
     if (tile_rows < 0) return set_error(GBSP_ERR_INVALID, "gbsp_execute_to_host: tile_rows must be >= 0");
-    const int tile = std::min(tile_rows > 0 ? tile_rows : 1024, p->u_tile);
+    const int tile = std::min(tile_rows > 0 ? tile_rows : p->stream_tile_auto, p->u_tile);
     cudaStream_t st = (cudaStream_t)stream;
     const size_t slab_bytes = (size_t)2 * tile * out_pitch * sizeof(float2);
     if (!p->stream_cs) {
@@ -1094,7 +1116,6 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
     for (int u0 = 0; u0 < p->half_rows && rc == GBSP_OK; u0 += tile, t++) {
         const int n = std::min(tile, p->half_rows - u0);
         const int b = t & 1;
-        if (t >= 2) GB_CUDA(cudaStreamWaitEvent(st, r.copied[b], 0));
         // rows u in [u0, u0+n) -> slab rows [0, n); their mirrors rows - u
         // (u >= 1, rows - u != u) form [hi_first, rows - u0] -> slab rows n..
         const int u_last = u0 + n - 1;
@@ -1103,6 +1124,9 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
         const int hi_last = p->rows - std::max(u0, 1);
         const int n_hi = std::max(0, hi_last - hi_first + 1);
         if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p->d_post, st))) break;
+        // only the row kernel writes the slab: pass 1 overlaps the copy
+        // that still drains it
+        if (t >= 2) GB_CUDA(cudaStreamWaitEvent(st, r.copied[b], 0));
         const gbsp::RowsArgs a =
             rows_args(p, p->d_S, p->s_pitch, u0, n, r.slab[b], out_pitch, u0 + n, u0, hi_first - n);
         if ((rc = launch_rows_args(p, a, st))) break;

@@ -11,6 +11,22 @@ namespace gbsp {
 // integers before it becomes a double angle.
 // ---------------------------------------------------------------------------
 
+// Row indices arrive as int32 in column order.  Each is checked against
+// [0, rows) -- any index outside sets *bad, and the plan is not built, so no
+// kernel ever reads a table with it -- and, when dst16 is given, stored as
+// u16.  Grid-stride; every thread reaches the warp vote.
+__global__ void k_row_index_in(const int* __restrict__ src, uint16_t* __restrict__ dst16, long nnz, int rows,
+                               int* bad) {
+    int b = 0;
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += stride) {
+        const int r = src[i];
+        b |= (unsigned)r >= (unsigned)rows;
+        if (dst16) dst16[i] = (uint16_t)r;
+    }
+    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
 // tab[p] = exp(-2*pi*i*p/rows), p < ntab
 // two_level: entries TWO_LO.. hold W^(TWO_LO*j) (layout of TAB_TWO)
 __global__ void k_table_rows(float2* __restrict__ tab, int ntab, int rows, int two_level) {

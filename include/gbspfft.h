@@ -62,6 +62,10 @@ enum { GBSP_PLANNER_MODEL = 0, GBSP_PLANNER_LEARNED = 1 };
 /* Length of the cost-model feature vector (gbsp_plan_features). */
 #define GBSP_N_FEATURES 36
 
+/* gbsp_options.stream_tile_rows: reserve the streaming slabs for the tile
+ * gbsp_execute_to_host picks when its tile_rows is 0. */
+#define GBSP_STREAM_TILE_AUTO (-1)
+
 typedef struct gbsp_plan_s* gbsp_plan_t;
 
 /* Tuning knobs.  Zero-initialise and set what you need; 0 means "default".
@@ -92,7 +96,8 @@ typedef struct {
                               (2 with 512-thread row blocks, else 1)                      */
     int stream_tile_rows;  /* > 0: reserve the two streaming slabs for tiles of this many
                               Bluestein rows in the plan's own allocation
-                              (gbsp_execute_to_host then allocates nothing)               */
+                              (gbsp_execute_to_host then allocates nothing);
+                              GBSP_STREAM_TILE_AUTO: reserve them for the automatic tile */
 } gbsp_options;
 
 typedef struct {
@@ -208,8 +213,10 @@ int gbsp_execute_noalloc(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* 
 /* Streams the transform to host memory: the reference's streaming methods
  * (sparse_fft_csc_stockham_streaming / _cufft_streaming,
  * src/sparse_fft_bluestein.cu:912-1145, 1150-1296), for outputs larger than
- * device memory.  Tiles of tile_rows Bluestein rows (0 = 1024, at most the
- * plan's u_tile) are computed into one of two device slabs holding the
+ * device memory.  Tiles of tile_rows Bluestein rows (at most the plan's
+ * u_tile; 0 = automatic: about a ninth of the rows, rounded to a multiple of
+ * the SM count, so the first tile's compute -- the part the copies cannot
+ * hide -- stays short while every row-kernel wave is full) are computed into one of two device slabs holding the
  * tile's output rows u and rows-u while the other slab is copied to h_out on
  * a second stream.  h_out: rows * out_pitch complex64 (pinned memory lets
  * the copies overlap); columns [cols/2+1, out_pitch) are written as zeros.

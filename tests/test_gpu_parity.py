@@ -92,6 +92,34 @@ def test_u_tiles_and_index_width(cuda):
         assert fp64.rel_l2(got, base) < 1e-5
 
 
+@pytest.mark.parametrize("index_bytes,u_tile", [(2, 0), (2, 1), (4, 0)])
+@pytest.mark.parametrize("bad", [-1, 100, 1 << 20])
+def test_row_index_out_of_range_is_rejected(cuda, index_bytes, u_tile, bad):
+    """Row indices are range-checked on the device while they upload (u16
+    narrowing staged in the scratch tile or, for a small tile, a region of its
+    own); a bad one fails the plan before any transform can read it."""
+    import ctypes as C
+    from cuspfft_gb300 import _capi
+    from cuspfft_gb300.sparse_fft import make_options
+    lib = _capi.load()
+    rows, cols, per_col = 100, 50, 12
+    g = np.random.default_rng(5)
+    ri = np.concatenate([np.sort(g.choice(rows, per_col, replace=False)) for _ in range(cols)]).astype(np.int32)
+    cp = np.arange(cols + 1, dtype=np.int32) * per_col
+    sc = np.arange(cols, dtype=np.int32)
+    o = make_options(None, index_bytes=index_bytes, u_tile=u_tile)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    h = C.c_void_p()
+    assert lib.gbsp_plan_create(rows, cols, cols, len(ri), ip(cp), ip(ri), ip(sc), C.byref(o), None,
+                                C.byref(h)) == _capi.GBSP_OK
+    assert lib.gbsp_plan_destroy(h) == _capi.GBSP_OK
+    ri[len(ri) // 2 + 3] = bad
+    h = C.c_void_p()
+    st = lib.gbsp_plan_create(rows, cols, cols, len(ri), ip(cp), ip(ri), ip(sc), C.byref(o), None, C.byref(h))
+    assert st == _capi.GBSP_ERR_INVALID and not h.value
+    assert "row index out of range" in _capi.last_error()
+
+
 def test_half_row_table(cuda):
     # rows beyond the full-table budget use the half-circle twiddle table
     coo = synthetic.uniform_matrix(24001, 40, 20000, seed=11)
