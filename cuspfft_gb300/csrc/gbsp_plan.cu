@@ -334,14 +334,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->rows_smem = rows_smem_bytes(p->fd);
     if ((rc = rows_prepare(p, sms))) return rc;
 
-    // ---- pass-1 task tables: each window's nonzeros cut into at most
-    // cw + P1_WARPS balanced tasks, longest first.  Built in one host buffer
-    // laid out like its device copy (slot0 | task | task_col), so one copy
-    // uploads it.
-    const int na = p->n_active;
-    std::vector<int> colp(p->cols + 1, 0);
-    for (int j = 0; j < na; j++) colp[sparse_cols[j] + 1] = col_ptr[j + 1] - col_ptr[j];
-    for (int c = 0; c < p->cols; c++) colp[c + 1] += colp[c];
+    // ---- pass-1 task tables (slot0 | task | task_col, one region): built on
+    // the device by k_p1_tasks from the column spans
     p->s_cols = (p->cols + 1) & ~1;
     const int CW = p->p1_cw, VM = gbsp::p1_vmax(p->p1_cw);
     const int n_win = (p->s_cols + CW - 1) / CW;
@@ -349,42 +343,6 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     const size_t off_task = (n_slot + 15) & ~(size_t)15;
     const size_t off_col = off_task + n_task * sizeof(int2);
     const size_t tbl_bytes = off_col + n_task;
-    std::vector<uint8_t> tbl(tbl_bytes, 0);
-    uint8_t* slot0 = tbl.data();
-    int2* task = reinterpret_cast<int2*>(tbl.data() + off_task);
-    uint8_t* task_col = tbl.data() + off_col;
-    struct Task { int b, e, col; };
-    std::vector<Task> ts(VM);
-    for (int w = 0; w < n_win; w++) {
-        auto deg = [&](int lc) {
-            const int c = w * CW + lc;
-            return c < p->cols ? colp[c + 1] - colp[c] : 0;
-        };
-        long sum = 0;
-        for (int lc = 0; lc < CW; lc++) sum += deg(lc);
-        const long T = std::max<long>(32, (sum + gbsp::P1_WARPS - 1) / gbsp::P1_WARPS);
-        int nt = 0;
-        for (int lc = 0; lc < CW; lc++) {
-            slot0[(size_t)w * (CW + 1) + lc] = (uint8_t)nt;
-            const int d = deg(lc);
-            if (d == 0) continue;
-            const int np = (int)((d + T - 1) / T);
-            if (nt + np > VM) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 window task overflow");
-            const int base = colp[w * CW + lc];
-            for (int k = 0; k < np; k++, nt++)
-                ts[nt] = {base + (int)((long)k * d / np), base + (int)((long)(k + 1) * d / np), nt};
-        }
-        slot0[(size_t)w * (CW + 1) + CW] = (uint8_t)nt;
-        // longest first, ties in creation order
-        std::sort(ts.begin(), ts.begin() + nt, [](const Task& a, const Task& b) {
-            const int la = a.e - a.b, lb = b.e - b.b;
-            return la != lb ? la > lb : a.col < b.col;
-        });
-        for (int i = 0; i < nt; i++) {
-            task[(size_t)w * VM + i] = make_int2(ts[i].b, ts[i].e);
-            task_col[(size_t)w * VM + i] = (uint8_t)ts[i].col;
-        }
-    }
     // one device allocation for every buffer of the plan
     {
         // automatic streaming tile: ~half_rows / 9, to the nearest multiple
@@ -398,10 +356,17 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     const size_t stream_slab = (size_t)2 * stream_tile * p->out_pitch * sizeof(float2);
     p->s_pitch = ((size_t)p->s_cols + 15) & ~(size_t)15;  // 128-byte rows; the bulk copy needs 16
     const size_t s_bytes = (size_t)p->u_tile * p->s_pitch * sizeof(float2);
-    // u16 indices are narrowed on the device from an int32 copy staged in the
-    // S tile, or in a region of their own when the tile is smaller
+    // the CSC arrives in a staging area -- the S tile, or a region of its own
+    // when the tile is smaller: [int32 row indices (u16 plans narrow them) |
+    // col_ptr | sparse_cols | column begin | column degree]
+    const int na = p->n_active;
+    auto a256 = [](size_t b) { return (std::max<size_t>(b, 16) + 255) & ~(size_t)255; };
     const size_t idx_in_bytes = (size_t)p->nnz * sizeof(int);
-    const size_t staging = (p->idx_bytes == 2 && idx_in_bytes > s_bytes) ? idx_in_bytes : 0;
+    const size_t st_row = (p->idx_bytes == 2) ? a256(idx_in_bytes) : 0;
+    const size_t st_cp = a256((size_t)(na + 1) * sizeof(int)), st_sc = a256((size_t)na * sizeof(int));
+    const size_t st_col = a256((size_t)p->cols * sizeof(int));
+    const size_t stage_bytes = st_row + st_cp + st_sc + 2 * st_col;
+    const size_t staging = stage_bytes > s_bytes ? stage_bytes : 0;
     {
         const int ntw_all = std::max(fft_tw_count(p->fd), 1);
         const size_t sizes[] = {tbl_bytes, (size_t)std::max(p->nnz, 1) * p->idx_bytes, 2 * sizeof(int),
@@ -442,16 +407,28 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2))))
         return rc;
     if ((rc = dev_alloc(p, &p->d_row_idx, (size_t)std::max(p->nnz, 1) * p->idx_bytes))) return rc;
-    if ((rc = dev_alloc(p, (void**)&p->d_err, 2 * sizeof(int)))) return rc;  // [1]: bad row index
+    // [1]: plan-build checks (bit 0 a row index out of range, bit 1 a task overflow)
+    if ((rc = dev_alloc(p, (void**)&p->d_err, 2 * sizeof(int)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_S, s_bytes))) return rc;
+    char* d_stage = reinterpret_cast<char*>(p->d_S);
+    if (staging > 0 && (rc = dev_alloc(p, (void**)&d_stage, staging))) return rc;
+    int* d_cp = reinterpret_cast<int*>(d_stage + st_row);
+    int* d_sc = reinterpret_cast<int*>(d_stage + st_row + st_cp);
+    int* d_cbeg = reinterpret_cast<int*>(d_stage + st_row + st_cp + st_sc);
+    int* d_deg = reinterpret_cast<int*>(d_stage + st_row + st_cp + st_sc + st_col);
     GB_CUDA(cudaMemsetAsync(p->d_err, 0, 2 * sizeof(int), st));
-    GB_CUDA(cudaMemcpyAsync(d_tbl, tbl.data(), tbl_bytes, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemsetAsync(d_deg, 0, (size_t)p->cols * sizeof(int), st));
+    GB_CUDA(cudaMemcpyAsync(d_cp, col_ptr, (size_t)(na + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (na > 0) {
+        GB_CUDA(cudaMemcpyAsync(d_sc, sparse_cols, (size_t)na * sizeof(int), cudaMemcpyHostToDevice, st));
+        gbsp::k_column_spans<<<blocks_for(na, 256), 256, 0, st>>>(d_cp, d_sc, na, d_cbeg, d_deg);
+        GB_CUDA(cudaGetLastError());
+    }
+    gbsp::k_p1_tasks<<<blocks_for(n_win, gbsp::TASK_WARPS), gbsp::TASK_WARPS * 32, 0, st>>>(
+        d_cbeg, d_deg, p->cols, CW, n_win, p->d_win_slot0, p->d_win_task, p->d_win_task_col, p->d_err + 1);
+    GB_CUDA(cudaGetLastError());
     if (p->nnz > 0) {
-        int* d_in = static_cast<int*>(p->d_row_idx);
-        if (p->idx_bytes == 2) {
-            d_in = reinterpret_cast<int*>(p->d_S);
-            if (staging > 0 && (rc = dev_alloc(p, (void**)&d_in, staging))) return rc;
-        }
+        int* d_in = (p->idx_bytes == 2) ? reinterpret_cast<int*>(d_stage) : static_cast<int*>(p->d_row_idx);
         GB_CUDA(cudaMemcpyAsync(d_in, row_idx, idx_in_bytes, cudaMemcpyHostToDevice, st));
         gbsp::k_row_index_in<<<(int)std::min<long>(blocks_for(p->nnz, 256), (long)sms * 8), 256, 0, st>>>(
             d_in, p->idx_bytes == 2 ? static_cast<uint16_t*>(p->d_row_idx) : nullptr, p->nnz, p->rows,
@@ -505,7 +482,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return set_error(GBSP_ERR_CUDA, std::string("plan tables: ") + cudaGetErrorString(e));
-    if (bad_row) return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: row index out of range");
+    if (bad_row & 1) return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: row index out of range");
+    if (bad_row & 2) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 window task overflow");
     return GBSP_OK;
 }
 

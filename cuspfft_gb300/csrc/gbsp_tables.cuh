@@ -27,6 +27,92 @@ __global__ void k_row_index_in(const int* __restrict__ src, uint16_t* __restrict
     if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
 }
 
+// Column c's first nonzero and degree from the compact CSC (deg[] zeroed
+// beforehand: columns without nonzeros stay 0).
+__global__ void k_column_spans(const int* __restrict__ col_ptr, const int* __restrict__ sparse_cols, int n_active,
+                               int* __restrict__ col_begin, int* __restrict__ deg) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_active) return;
+    const int c = sparse_cols[j];
+    col_begin[c] = col_ptr[j];
+    deg[c] = col_ptr[j + 1] - col_ptr[j];
+}
+
+// Pass-1 task tables, one warp per window of cw (32 or 64) columns.  With
+// T = max(32, ceil(window nonzeros / P1_WARPS)), column lc splits into
+// np = ceil(deg / T) tasks at nonzero offsets floor(k * deg / np); the tasks
+// take tile columns (slots) in column order, slot0[lc] being column lc's
+// first (slot0[cw] = the window's task count), and are listed longest first,
+// ties in slot order.  np sums to < window nonzeros / T + cw <= cw + P1_WARPS,
+// so the vmax-long list cannot overflow (a violation would set *bad, bit 1).
+constexpr int TASK_WARPS = 4;
+__global__ void __launch_bounds__(TASK_WARPS * 32)
+k_p1_tasks(const int* __restrict__ col_begin, const int* __restrict__ deg, int cols, int cw, int n_win,
+           uint8_t* __restrict__ slot0, int2* __restrict__ task, uint8_t* __restrict__ task_col, int* bad) {
+    __shared__ int2 s_task[TASK_WARPS][64 + P1_WARPS];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * TASK_WARPS + wl;
+    if (w >= n_win) return;  // warp-uniform
+    const int vmax = p1_vmax(cw);
+    const int halves = cw / 32;  // columns lane and lane + 32
+    int d[2] = {0, 0};
+    for (int h = 0; h < halves; h++) {
+        const int c = w * cw + h * 32 + lane;
+        d[h] = c < cols ? deg[c] : 0;
+    }
+    int sum = d[0] + d[1];
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    const int T = max(32, (sum + P1_WARPS - 1) / P1_WARPS);
+    int first[2] = {0, 0}, np[2] = {0, 0};
+    int base = 0;
+    for (int h = 0; h < halves; h++) {
+        np[h] = (d[h] + T - 1) / T;
+        int incl = np[h];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        first[h] = base + incl - np[h];
+        base += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    const int nt = base;
+    uint8_t* s0 = slot0 + (size_t)w * (cw + 1);
+    for (int h = 0; h < halves; h++) s0[h * 32 + lane] = (uint8_t)min(first[h], vmax);
+    if (lane == 0) s0[cw] = (uint8_t)min(nt, vmax);
+    if (nt > vmax) {
+        if (lane == 0) atomicOr(bad, 2);
+        return;
+    }
+    for (int h = 0; h < halves; h++) {
+        const int c = w * cw + h * 32 + lane;
+        if (np[h] == 0) continue;
+        const int b0 = col_begin[c];
+        for (int k = 0; k < np[h]; k++)
+            s_task[wl][first[h] + k] = make_int2(b0 + (int)((long long)k * d[h] / np[h]),
+                                                 b0 + (int)((long long)(k + 1) * d[h] / np[h]));
+    }
+    __syncwarp();
+    int2* tw = task + (size_t)w * vmax;
+    uint8_t* tc = task_col + (size_t)w * vmax;
+    for (int i = lane; i < vmax; i += 32) {
+        if (i >= nt) {
+            tw[i] = make_int2(0, 0);
+            tc[i] = 0;
+        }
+    }
+    for (int i = lane; i < nt; i += 32) {
+        const int2 t = s_task[wl][i];
+        const int len = t.y - t.x;
+        int rank = 0;
+        for (int j = 0; j < nt; j++) {
+            const int lj = s_task[wl][j].y - s_task[wl][j].x;
+            rank += (lj > len) || (lj == len && j < i);
+        }
+        tw[rank] = t;
+        tc[rank] = (uint8_t)i;
+    }
+}
+
 // tab[p] = exp(-2*pi*i*p/rows), p < ntab
 // two_level: entries TWO_LO.. hold W^(TWO_LO*j) (layout of TAB_TWO)
 __global__ void k_table_rows(float2* __restrict__ tab, int ntab, int rows, int two_level) {
