@@ -7,11 +7,11 @@ hand-written CUDA kernels behind a C ABI (include/gbspfft.h).
 """
 from ._capi import GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GBSP_STREAM_TILE_AUTO, GbspError, LIB_PATH, load
 from .sparse_fft import (Batch, COOMatrix, CompactCSC, Plan, SparseFFTResult, make_compact_csc, next_smooth,
-                         read_mtx, sparse_fft_csc_bluestein_cufft_smooth,
+                         read_mtx, set_memory_cache, sparse_fft_csc_bluestein_cufft_smooth,
                          sparse_fft_csc_bluestein_mixed_radix)
 
 __all__ = [
     "GBSP_LEN_3SMOOTH", "GBSP_LEN_7SMOOTH", "GBSP_STREAM_TILE_AUTO", "GbspError", "LIB_PATH", "load", "Batch",
     "COOMatrix", "CompactCSC", "Plan", "SparseFFTResult", "make_compact_csc", "next_smooth", "read_mtx",
-    "sparse_fft_csc_bluestein_cufft_smooth", "sparse_fft_csc_bluestein_mixed_radix",
+    "set_memory_cache", "sparse_fft_csc_bluestein_cufft_smooth", "sparse_fft_csc_bluestein_mixed_radix",
 ]

@@ -38,7 +38,7 @@ EXPORTED = (
     "gbsp_batch_execute", "gbsp_batch_graph_launch", "gbsp_batch_plan_info", "gbsp_batch_error_flags",
     "gbsp_batch_destroy", "gbsp_plan_candidates", "gbsp_plan_features", "gbsp_autotune", "gbsp_mlp_param_count",
     "gbsp_mlp_forward", "gbsp_mlp_work_floats", "gbsp_mlp_backward", "gbsp_mlp_adam", "gbsp_cost_model_set",
-    "gbsp_execute_to_host",
+    "gbsp_execute_to_host", "gbsp_set_memory_cache",
 )
 
 
@@ -124,6 +124,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                      C.POINTER(vp)]
     lib.gbsp_plan_get_info.argtypes = [vp, C.POINTER(GbspPlanInfo)]
     lib.gbsp_plan_destroy.argtypes = [vp]
+    lib.gbsp_set_memory_cache.argtypes = [C.c_size_t]
     lib.gbsp_execute.argtypes = [vp, vp, C.c_size_t, vp]
     lib.gbsp_execute_profiled.argtypes = [vp, vp, C.c_size_t, vp, C.POINTER(C.c_float),
                                            C.POINTER(C.c_float)]

@@ -73,6 +73,7 @@ struct gbsp_plan_s {
     size_t stream_slab_bytes = 0;
     int stream_tile_auto = 1;        // tile_rows 0 of gbsp_execute_to_host
     bool stream_slab_owned = false;  // allocated on first use (else carved from the arena)
+    bool arena_pooled = false;       // arena from the library's memory pool (else cudaMalloc)
 };
 
 namespace {
@@ -98,8 +99,45 @@ int dev_alloc(gbsp_plan_s* p, void** ptr, size_t bytes) {
     return GBSP_OK;
 }
 
+// ---- plan memory: one stream-ordered pool per device, private to the
+// library, that keeps up to g_cache_limit bytes of freed plan memory for the
+// next plan (a cudaMalloc and a cudaFree of a plan's arena cost ~0.1 ms each)
+constexpr int MAX_POOL_DEVICES = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[MAX_POOL_DEVICES] = {};
+unsigned long long g_cache_limit = 1ull << 30;
+
+// *pool = the device's plan pool (created on first use), or nullptr for a
+// device number the table does not cover (plain cudaMalloc then)
+int plan_pool(int dev, cudaMemPool_t* pool) {
+    *pool = nullptr;
+    if (dev < 0 || dev >= MAX_POOL_DEVICES) return GBSP_OK;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t mp = nullptr;
+        GB_CUDA(cudaMemPoolCreate(&mp, &props));
+        unsigned long long thr = g_cache_limit;
+        GB_CUDA(cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &thr));
+        g_pool[dev] = mp;
+    }
+    *pool = g_pool[dev];
+    return GBSP_OK;
+}
+
 void free_plan(gbsp_plan_s* p) {
     if (!p) return;
+    if (p->arena && p->arena_pooled) {
+        // the plan's kernels may run on any stream: wait for the device, as
+        // cudaFree would, before the arena goes back to the pool
+        cudaDeviceSynchronize();
+        cudaFreeAsync(p->arena, 0);
+        cudaStreamSynchronize(0);
+    }
     for (void* a : p->allocs) cudaFree(a);
     for (int b = 0; b < 2; b++) {
         if (p->stream_slab[b] && p->stream_slab_owned) cudaFree(p->stream_slab[b]);
@@ -381,13 +419,18 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         size_t total = 0;
         for (size_t b : sizes) total += (std::max<size_t>(b, 16) + 255) & ~(size_t)255;
         void* base = nullptr;
-        cudaError_t e = cudaMalloc(&base, total);
+        cudaMemPool_t pool = nullptr;
+        if ((rc = plan_pool(p->device, &pool))) return rc;
+        cudaError_t e = pool ? cudaMallocFromPoolAsync(&base, total, pool, st) : cudaMalloc(&base, total);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            return set_error(GBSP_ERR_ALLOC, std::string("cudaMalloc(") + std::to_string(total) +
-                                                 "): " + cudaGetErrorString(e));
+            return set_error(GBSP_ERR_ALLOC, std::string("plan memory (") + std::to_string(total) +
+                                                 " bytes): " + cudaGetErrorString(e));
         }
-        p->allocs.push_back(base);
+        if (pool)
+            p->arena_pooled = true;
+        else
+            p->allocs.push_back(base);
         p->device_bytes += total;
         p->arena = static_cast<char*>(base);
         p->arena_size = total;
@@ -519,6 +562,18 @@ int gbsp_plan_create(int rows, int cols, int n_active, int nnz, const int* col_p
         return rc;
     }
     *plan = p;
+    return GBSP_OK;
+}
+
+int gbsp_set_memory_cache(size_t bytes) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    g_cache_limit = bytes;
+    for (int d = 0; d < MAX_POOL_DEVICES; d++) {
+        if (!g_pool[d]) continue;
+        unsigned long long thr = bytes;
+        GB_CUDA(cudaMemPoolSetAttribute(g_pool[d], cudaMemPoolAttrReleaseThreshold, &thr));
+        GB_CUDA(cudaMemPoolTrimTo(g_pool[d], bytes));
+    }
     return GBSP_OK;
 }
 

@@ -96,6 +96,12 @@ def next_smooth(n: int, policy: int = GBSP_LEN_3SMOOTH) -> int:
     return int(load().gbsp_next_smooth(int(n), int(policy)))
 
 
+def set_memory_cache(nbytes: int) -> None:
+    """Freed plan memory the library's pool keeps for later plans, per device
+    (default 1 GiB); 0 keeps nothing."""
+    check(load().gbsp_set_memory_cache(int(nbytes)), "gbsp_set_memory_cache")
+
+
 def _stream_handle(stream) -> Optional[int]:
     """cudaStream_t of a torch stream; torch's current stream when None (the
     legacy default stream if CUDA is unavailable -- the library then reports

@@ -156,12 +156,24 @@ int gbsp_next_smooth(int n, int policy);
  * twiddles: FP64 on the GPU, rounded to FP32) and uploads the CSC.  Host
  * arrays in, device state out; this is the reference's untimed setup
  * (src/sparse_fft_bluestein.cu:2263-2321).  `stream` is a cudaStream_t
- * (NULL = legacy default stream). */
+ * (NULL = legacy default stream).  Row indices are range-checked on the
+ * device during the upload (GBSP_ERR_INVALID when one is outside [0, rows)).
+ * The plan's device memory is one allocation from a stream-ordered pool
+ * private to the library (see gbsp_set_memory_cache). */
 int gbsp_plan_create(int rows, int cols, int n_active, int nnz,
                      const int* col_ptr, const int* row_idx, const int* sparse_cols,
                      const gbsp_options* opts, void* stream, gbsp_plan_t* plan);
 int gbsp_plan_get_info(gbsp_plan_t plan, gbsp_plan_info* info);
+/* Waits for the device (as cudaFree does) and returns the plan's memory to
+ * the pool. */
 int gbsp_plan_destroy(gbsp_plan_t plan);
+
+/* Freed plan memory the library's pool keeps for later plans, per device
+ * (default 1 GiB): a cudaMalloc and a cudaFree of a plan's allocation cost
+ * ~0.1 ms each, a pooled one a few microseconds.  Memory above the limit
+ * goes back to the driver at the next synchronisation; 0 keeps nothing.
+ * Takes effect at once (trims the pools to the new limit). */
+int gbsp_set_memory_cache(size_t bytes);
 
 /* Runs the transform: the reference's timed tile loop
  * (src/sparse_fft_bluestein.cu:2327-2370).  d_out is device memory of at
