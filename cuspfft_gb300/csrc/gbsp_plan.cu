@@ -129,6 +129,18 @@ int plan_pool(int dev, cudaMemPool_t* pool) {
     return GBSP_OK;
 }
 
+// *hs = the device's helper stream for plan-build work that runs beside the
+// caller's stream (created on first use), or nullptr (run on the caller's)
+cudaStream_t g_helper[MAX_POOL_DEVICES] = {};
+int helper_stream(int dev, cudaStream_t* hs) {
+    *hs = nullptr;
+    if (dev < 0 || dev >= MAX_POOL_DEVICES) return GBSP_OK;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_helper[dev]) GB_CUDA(cudaStreamCreateWithFlags(&g_helper[dev], cudaStreamNonBlocking));
+    *hs = g_helper[dev];
+    return GBSP_OK;
+}
+
 void free_plan(gbsp_plan_s* p) {
     if (!p) return;
     if (p->arena && p->arena_pooled) {
@@ -373,7 +385,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     if ((rc = rows_prepare(p, sms))) return rc;
 
     // ---- pass-1 task tables (slot0 | task | task_col, one region): built on
-    // the device by k_p1_tasks from the column spans
+    // the device by k_csc_setup from the compact CSC
     p->s_cols = (p->cols + 1) & ~1;
     const int CW = p->p1_cw, VM = gbsp::p1_vmax(p->p1_cw);
     const int n_win = (p->s_cols + CW - 1) / CW;
@@ -396,28 +408,28 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     const size_t s_bytes = (size_t)p->u_tile * p->s_pitch * sizeof(float2);
     // the CSC arrives in a staging area -- the S tile, or a region of its own
     // when the tile is smaller: [int32 row indices (u16 plans narrow them) |
-    // col_ptr | sparse_cols | column begin | column degree]
+    // col_ptr | sparse_cols]
     const int na = p->n_active;
     auto a256 = [](size_t b) { return (std::max<size_t>(b, 16) + 255) & ~(size_t)255; };
     const size_t idx_in_bytes = (size_t)p->nnz * sizeof(int);
     const size_t st_row = (p->idx_bytes == 2) ? a256(idx_in_bytes) : 0;
     const size_t st_cp = a256((size_t)(na + 1) * sizeof(int)), st_sc = a256((size_t)na * sizeof(int));
-    const size_t st_col = a256((size_t)p->cols * sizeof(int));
-    const size_t stage_bytes = st_row + st_cp + st_sc + 2 * st_col;
+    const size_t stage_bytes = st_row + st_cp + st_sc;
     const size_t staging = stage_bytes > s_bytes ? stage_bytes : 0;
+    const int K = p->K, Lp = p->Lp, cols = p->cols;
+    const int ntw = std::max(fft_tw_count(p->fd), 1);
     {
-        const int ntw_all = std::max(fft_tw_count(p->fd), 1);
         const size_t sizes[] = {tbl_bytes, (size_t)std::max(p->nnz, 1) * p->idx_bytes, 2 * sizeof(int),
-                                (size_t)p->ntab * sizeof(float2), (size_t)p->K * p->cols * sizeof(float2),
-                                (size_t)p->K * p->cols * sizeof(float2), (size_t)p->K * p->Lp * sizeof(float2),
-                                (size_t)ntw_all * sizeof(float2), (size_t)p->K * p->Lp * sizeof(double2),
-                                (size_t)p->K * p->Lp * sizeof(double2), s_bytes, staging,
+                                (size_t)p->ntab * sizeof(float2), (size_t)K * cols * sizeof(float2),
+                                (size_t)K * cols * sizeof(float2), (size_t)K * Lp * sizeof(float2),
+                                (size_t)ntw * sizeof(float2), (size_t)K * Lp * sizeof(double2),
+                                (size_t)K * Lp * sizeof(double2), s_bytes, staging,
                                 (p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW)
-                                    ? (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2)
+                                    ? (size_t)p->rows_grid * (K - 1) * Lp * sizeof(float2)
                                     : 0,
                                 stream_slab, stream_slab};
         size_t total = 0;
-        for (size_t b : sizes) total += (std::max<size_t>(b, 16) + 255) & ~(size_t)255;
+        for (size_t b : sizes) total += a256(b);
         void* base = nullptr;
         cudaMemPool_t pool = nullptr;
         if ((rc = plan_pool(p->device, &pool))) return rc;
@@ -447,7 +459,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         p->stream_slab_bytes = stream_slab;
     }
     if ((p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW) &&
-        (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (p->K - 1) * p->Lp * sizeof(float2))))
+        (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (K - 1) * Lp * sizeof(float2))))
         return rc;
     if ((rc = dev_alloc(p, &p->d_row_idx, (size_t)std::max(p->nnz, 1) * p->idx_bytes))) return rc;
     // [1]: plan-build checks (bit 0 a row index out of range, bit 1 a task overflow)
@@ -455,78 +467,113 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     if ((rc = dev_alloc(p, (void**)&p->d_S, s_bytes))) return rc;
     char* d_stage = reinterpret_cast<char*>(p->d_S);
     if (staging > 0 && (rc = dev_alloc(p, (void**)&d_stage, staging))) return rc;
-    int* d_cp = reinterpret_cast<int*>(d_stage + st_row);
-    int* d_sc = reinterpret_cast<int*>(d_stage + st_row + st_cp);
-    int* d_cbeg = reinterpret_cast<int*>(d_stage + st_row + st_cp + st_sc);
-    int* d_deg = reinterpret_cast<int*>(d_stage + st_row + st_cp + st_sc + st_col);
-    GB_CUDA(cudaMemsetAsync(p->d_err, 0, 2 * sizeof(int), st));
-    GB_CUDA(cudaMemsetAsync(d_deg, 0, (size_t)p->cols * sizeof(int), st));
-    GB_CUDA(cudaMemcpyAsync(d_cp, col_ptr, (size_t)(na + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
-    if (na > 0) {
-        GB_CUDA(cudaMemcpyAsync(d_sc, sparse_cols, (size_t)na * sizeof(int), cudaMemcpyHostToDevice, st));
-        gbsp::k_column_spans<<<blocks_for(na, 256), 256, 0, st>>>(d_cp, d_sc, na, d_cbeg, d_deg);
-        GB_CUDA(cudaGetLastError());
-    }
-    gbsp::k_p1_tasks<<<blocks_for(n_win, gbsp::TASK_WARPS), gbsp::TASK_WARPS * 32, 0, st>>>(
-        d_cbeg, d_deg, p->cols, CW, n_win, p->d_win_slot0, p->d_win_task, p->d_win_task_col, p->d_err + 1);
-    GB_CUDA(cudaGetLastError());
-    if (p->nnz > 0) {
-        int* d_in = (p->idx_bytes == 2) ? reinterpret_cast<int*>(d_stage) : static_cast<int*>(p->d_row_idx);
-        GB_CUDA(cudaMemcpyAsync(d_in, row_idx, idx_in_bytes, cudaMemcpyHostToDevice, st));
-        gbsp::k_row_index_in<<<(int)std::min<long>(blocks_for(p->nnz, 256), (long)sms * 8), 256, 0, st>>>(
-            d_in, p->idx_bytes == 2 ? static_cast<uint16_t*>(p->d_row_idx) : nullptr, p->nnz, p->rows,
-            p->d_err + 1);
-        GB_CUDA(cudaGetLastError());
-    }
-
-    // ---- tables (FP64 on the device, rounded to FP32)
-    const int K = p->K, Lp = p->Lp, cols = p->cols;
     if ((rc = dev_alloc(p, (void**)&p->d_rowtab, (size_t)p->ntab * sizeof(float2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_pre, (size_t)K * cols * sizeof(float2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_post, (size_t)K * cols * sizeof(float2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_filt, (size_t)K * Lp * sizeof(float2)))) return rc;
-    const int ntw = std::max(fft_tw_count(p->fd), 1);
     if ((rc = dev_alloc(p, (void**)&p->d_fftw, (size_t)ntw * sizeof(float2)))) return rc;
-
-    gbsp::k_table_rows<<<blocks_for(p->ntab, 256), 256, 0, st>>>(p->d_rowtab, p->ntab, p->rows,
-                                                                 p->tab_mode == gbsp::TAB_TWO);
-    GB_CUDA(cudaGetLastError());
-    gbsp::k_table_pre<<<blocks_for((long)K * cols, 256), 256, 0, st>>>(p->d_pre, cols, p->L, K);
-    GB_CUDA(cudaGetLastError());
-    gbsp::k_table_post<<<blocks_for((long)K * cols, 256), 256, 0, st>>>(p->d_post, cols, p->L, K);
-    GB_CUDA(cudaGetLastError());
-    for (int s = 0; s < p->fd.nst; s++) {
-        const int n = (p->fd.R[s] - 1) * p->fd.m[s];
-        if (n == 0) continue;
-        gbsp::k_table_fft<<<blocks_for(n, 256), 256, 0, st>>>(p->d_fftw, Lp, p->fd.R[s], p->fd.m[s],
-                                                               p->fd.twoff[s]);
-        GB_CUDA(cudaGetLastError());
-    }
-    // FP64 filter workspace, kept with the plan (freeing it here would
-    // synchronise the whole device)
-    double2* d_spec[2] = {nullptr, nullptr};  // ping-pong: the stages run out of place
+    // FP64 filter workspace (ping-pong: the stages run out of place), kept
+    // with the plan: freeing it here would synchronise the whole device
+    double2* d_spec[2] = {nullptr, nullptr};
     if ((rc = dev_alloc(p, (void**)&d_spec[0], (size_t)K * Lp * sizeof(double2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&d_spec[1], (size_t)K * Lp * sizeof(double2)))) return rc;
-    gbsp::k_table_filter_input<<<blocks_for((long)K * Lp, 256), 256, 0, st>>>(d_spec[0], cols, p->L, K, Lp);
+
+    // ---- device work.  The tables (FP64, rounded to FP32) and the filter
+    // spectrum (input, DIF stages, final rounding: a chain of dependent
+    // launches) need nothing from the host, so they run on the library's
+    // helper stream beside the CSC uploads and their setup kernel on `st`;
+    // the two join before the synchronisation.
+    cudaStream_t hs = nullptr;
+    if ((rc = helper_stream(p->device, &hs))) return rc;
+    struct Events {  // fork / join, released on every return path
+        cudaEvent_t e[2] = {nullptr, nullptr};
+        ~Events() {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } evs;
+    cudaEvent_t* ev = evs.e;
+    cudaStream_t fs = st;
+    if (hs) {
+        GB_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+        GB_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+        GB_CUDA(cudaEventRecord(ev[0], st));  // after the arena's stream-ordered allocation
+        GB_CUDA(cudaStreamWaitEvent(hs, ev[0], 0));
+        fs = hs;
+    }
+    {
+        gbsp::TableArgs ta;
+        ta.rowtab = p->d_rowtab;
+        ta.pre = p->d_pre;
+        ta.post = p->d_post;
+        ta.fftw = p->d_fftw;
+        ta.ntab = p->ntab;
+        ta.rows = p->rows;
+        ta.two_level = p->tab_mode == gbsp::TAB_TWO;
+        ta.cols = cols;
+        ta.L = p->L;
+        ta.K = K;
+        ta.fd = p->fd;
+        const long n_tab = (long)p->ntab + 2L * K * cols + fft_tw_count(p->fd);
+        gbsp::k_tables<<<blocks_for(n_tab, 256), 256, 0, fs>>>(ta);
+    }
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        gbsp::k_table_filter_input<<<blocks_for((long)K * Lp, 256), 256, 0, fs>>>(d_spec[0], cols, p->L, K, Lp);
+        e = cudaGetLastError();
+    }
     int cur = 0;
     for (int s = 0; s < p->fd.nst && e == cudaSuccess; s++, cur ^= 1) {
-        gbsp::k_dif_stage_f64<<<blocks_for((long)K * Lp, 128), 128, 0, st>>>(d_spec[cur], d_spec[cur ^ 1], K, Lp,
+        gbsp::k_dif_stage_f64<<<blocks_for((long)K * Lp, 128), 128, 0, fs>>>(d_spec[cur], d_spec[cur ^ 1], K, Lp,
                                                                              p->fd.R[s], p->fd.m[s]);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
-        gbsp::k_table_filter_final<<<blocks_for((long)K * Lp, 256), 256, 0, st>>>(
+        gbsp::k_table_filter_final<<<blocks_for((long)K * Lp, 256), 256, 0, fs>>>(
             p->d_filt, d_spec[cur], K, Lp, p->fd.R[p->fd.nst - 1], 1.0 / (double)p->L);
         e = cudaGetLastError();
     }
-    int bad_row = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad_row, p->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (hs && e == cudaSuccess) e = cudaEventRecord(ev[1], hs);
+    // the CSC: uploads, then one setup kernel (task tables, row-index check)
+    int* d_cp = reinterpret_cast<int*>(d_stage + st_row);
+    int* d_sc = reinterpret_cast<int*>(d_stage + st_row + st_cp);
+    int* d_in = (p->idx_bytes == 2) ? reinterpret_cast<int*>(d_stage) : static_cast<int*>(p->d_row_idx);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->d_err, 0, 2 * sizeof(int), st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_cp, col_ptr, (size_t)(na + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && na > 0)
+        e = cudaMemcpyAsync(d_sc, sparse_cols, (size_t)na * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && p->nnz > 0) e = cudaMemcpyAsync(d_in, row_idx, idx_in_bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        gbsp::CscSetupArgs ca;
+        ca.col_ptr = d_cp;
+        ca.sparse_cols = d_sc;
+        ca.n_active = na;
+        ca.cols = cols;
+        ca.cw = CW;
+        ca.n_win = n_win;
+        ca.task_blocks = (int)blocks_for(n_win, gbsp::SETUP_WARPS);
+        ca.slot0 = p->d_win_slot0;
+        ca.task = p->d_win_task;
+        ca.task_col = p->d_win_task_col;
+        ca.row_in = d_in;
+        ca.row16 = (p->idx_bytes == 2) ? static_cast<uint16_t*>(p->d_row_idx) : nullptr;
+        ca.nnz = p->nnz;
+        ca.rows = p->rows;
+        ca.bad = p->d_err + 1;
+        const int row_blocks = (int)std::min<long>(blocks_for(p->nnz, gbsp::SETUP_WARPS * 32), (long)sms * 16);
+        gbsp::k_csc_setup<<<ca.task_blocks + std::max(row_blocks, 1), gbsp::SETUP_WARPS * 32, 0, st>>>(ca);
+        e = cudaGetLastError();
+    }
+    if (hs && e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[1], 0);
+    int bad = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, p->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (hs && e != cudaSuccess) cudaStreamSynchronize(hs);  // nothing of this plan may still run
     if (e != cudaSuccess)
-        return set_error(GBSP_ERR_CUDA, std::string("plan tables: ") + cudaGetErrorString(e));
-    if (bad_row & 1) return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: row index out of range");
-    if (bad_row & 2) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 window task overflow");
+        return set_error(GBSP_ERR_CUDA, std::string("plan build: ") + cudaGetErrorString(e));
+    if (bad & 1) return set_error(GBSP_ERR_INVALID, "gbsp_plan_create: row index out of range");
+    if (bad & 2) return set_error(GBSP_ERR_UNSUPPORTED, "pass-1 window task overflow");
     return GBSP_OK;
 }
 

@@ -11,55 +11,79 @@ namespace gbsp {
 // integers before it becomes a double angle.
 // ---------------------------------------------------------------------------
 
-// Row indices arrive as int32 in column order.  Each is checked against
-// [0, rows) -- any index outside sets *bad, and the plan is not built, so no
-// kernel ever reads a table with it -- and, when dst16 is given, stored as
-// u16.  Grid-stride; every thread reaches the warp vote.
-__global__ void k_row_index_in(const int* __restrict__ src, uint16_t* __restrict__ dst16, long nnz, int rows,
-                               int* bad) {
-    int b = 0;
-    const long stride = (long)gridDim.x * blockDim.x;
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += stride) {
-        const int r = src[i];
-        b |= (unsigned)r >= (unsigned)rows;
-        if (dst16) dst16[i] = (uint16_t)r;
-    }
-    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
-}
-
-// Column c's first nonzero and degree from the compact CSC (deg[] zeroed
-// beforehand: columns without nonzeros stay 0).
-__global__ void k_column_spans(const int* __restrict__ col_ptr, const int* __restrict__ sparse_cols, int n_active,
-                               int* __restrict__ col_begin, int* __restrict__ deg) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_active) return;
-    const int c = sparse_cols[j];
-    col_begin[c] = col_ptr[j];
-    deg[c] = col_ptr[j + 1] - col_ptr[j];
-}
-
-// Pass-1 task tables, one warp per window of cw (32 or 64) columns.  With
+// The CSC half of a plan's build, one launch:
+//
+// Blocks [0, task_blocks): the pass-1 task tables, one warp per window of cw
+// (32 or 64) columns.  The window's active columns are found in sparse_cols
+// (strictly increasing) by a binary search for its first column.  With
 // T = max(32, ceil(window nonzeros / P1_WARPS)), column lc splits into
 // np = ceil(deg / T) tasks at nonzero offsets floor(k * deg / np); the tasks
 // take tile columns (slots) in column order, slot0[lc] being column lc's
 // first (slot0[cw] = the window's task count), and are listed longest first,
 // ties in slot order.  np sums to < window nonzeros / T + cw <= cw + P1_WARPS,
 // so the vmax-long list cannot overflow (a violation would set *bad, bit 1).
-constexpr int TASK_WARPS = 4;
-__global__ void __launch_bounds__(TASK_WARPS * 32)
-k_p1_tasks(const int* __restrict__ col_begin, const int* __restrict__ deg, int cols, int cw, int n_win,
-           uint8_t* __restrict__ slot0, int2* __restrict__ task, uint8_t* __restrict__ task_col, int* bad) {
-    __shared__ int2 s_task[TASK_WARPS][64 + P1_WARPS];
-    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int w = blockIdx.x * TASK_WARPS + wl;
-    if (w >= n_win) return;  // warp-uniform
-    const int vmax = p1_vmax(cw);
-    const int halves = cw / 32;  // columns lane and lane + 32
-    int d[2] = {0, 0};
-    for (int h = 0; h < halves; h++) {
-        const int c = w * cw + h * 32 + lane;
-        d[h] = c < cols ? deg[c] : 0;
+//
+// Blocks [task_blocks, gridDim.x): the row indices, int32 in column order,
+// each checked against [0, rows) -- one outside sets *bad (bit 0) and the
+// plan is not built, so no kernel ever reads a table with it -- and, when
+// row16 is given, stored as u16.  Grid-stride; every thread of these blocks
+// reaches the warp vote.
+constexpr int SETUP_WARPS = 4;
+struct CscSetupArgs {
+    const int* col_ptr;      // n_active + 1
+    const int* sparse_cols;  // n_active, strictly increasing
+    int n_active, cols, cw, n_win, task_blocks;
+    uint8_t* slot0;
+    int2* task;
+    uint8_t* task_col;
+    const int* row_in;  // nnz int32
+    uint16_t* row16;    // nullptr: 4-byte indices, checked in place
+    long nnz;
+    int rows;
+    int* bad;
+};
+__global__ void __launch_bounds__(SETUP_WARPS * 32) k_csc_setup(CscSetupArgs a) {
+    if ((int)blockIdx.x >= a.task_blocks) {
+        int b = 0;
+        const long stride = (long)(gridDim.x - a.task_blocks) * blockDim.x;
+        for (long i = (long)(blockIdx.x - a.task_blocks) * blockDim.x + threadIdx.x; i < a.nnz; i += stride) {
+            const int r = a.row_in[i];
+            b |= (unsigned)r >= (unsigned)a.rows;
+            if (a.row16) a.row16[i] = (uint16_t)r;
+        }
+        if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(a.bad, 1);
+        return;
     }
+    __shared__ int2 s_task[SETUP_WARPS][64 + P1_WARPS];
+    __shared__ int s_deg[SETUP_WARPS][64], s_beg[SETUP_WARPS][64];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * SETUP_WARPS + wl;
+    if (w >= a.n_win) return;  // warp-uniform
+    const int cw = a.cw, vmax = p1_vmax(cw);
+    const int halves = cw / 32;  // columns lane and lane + 32
+    const int c0 = w * cw;
+    // first active column >= c0
+    int lo = 0, hi = a.n_active;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a.sparse_cols[mid] < c0) lo = mid + 1;
+        else hi = mid;
+    }
+    for (int h = 0; h < halves; h++) s_deg[wl][h * 32 + lane] = 0;
+    __syncwarp();
+    for (int h = 0; h < halves; h++) {
+        const int j = lo + h * 32 + lane;
+        if (j < a.n_active) {
+            const int c = a.sparse_cols[j];
+            if (c < c0 + cw) {
+                s_deg[wl][c - c0] = a.col_ptr[j + 1] - a.col_ptr[j];
+                s_beg[wl][c - c0] = a.col_ptr[j];
+            }
+        }
+    }
+    __syncwarp();
+    int d[2] = {0, 0};
+    for (int h = 0; h < halves; h++) d[h] = s_deg[wl][h * 32 + lane];
     int sum = d[0] + d[1];
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     const int T = max(32, (sum + P1_WARPS - 1) / P1_WARPS);
@@ -76,29 +100,26 @@ k_p1_tasks(const int* __restrict__ col_begin, const int* __restrict__ deg, int c
         base += __shfl_sync(0xffffffffu, incl, 31);
     }
     const int nt = base;
-    uint8_t* s0 = slot0 + (size_t)w * (cw + 1);
+    uint8_t* s0 = a.slot0 + (size_t)w * (cw + 1);
     for (int h = 0; h < halves; h++) s0[h * 32 + lane] = (uint8_t)min(first[h], vmax);
     if (lane == 0) s0[cw] = (uint8_t)min(nt, vmax);
     if (nt > vmax) {
-        if (lane == 0) atomicOr(bad, 2);
+        if (lane == 0) atomicOr(a.bad, 2);
         return;
     }
     for (int h = 0; h < halves; h++) {
-        const int c = w * cw + h * 32 + lane;
         if (np[h] == 0) continue;
-        const int b0 = col_begin[c];
+        const int b0 = s_beg[wl][h * 32 + lane];
         for (int k = 0; k < np[h]; k++)
             s_task[wl][first[h] + k] = make_int2(b0 + (int)((long long)k * d[h] / np[h]),
                                                  b0 + (int)((long long)(k + 1) * d[h] / np[h]));
     }
     __syncwarp();
-    int2* tw = task + (size_t)w * vmax;
-    uint8_t* tc = task_col + (size_t)w * vmax;
-    for (int i = lane; i < vmax; i += 32) {
-        if (i >= nt) {
-            tw[i] = make_int2(0, 0);
-            tc[i] = 0;
-        }
+    int2* tw = a.task + (size_t)w * vmax;
+    uint8_t* tc = a.task_col + (size_t)w * vmax;
+    for (int i = nt + lane; i < vmax; i += 32) {
+        tw[i] = make_int2(0, 0);
+        tc[i] = 0;
     }
     for (int i = lane; i < nt; i += 32) {
         const int2 t = s_task[wl][i];
@@ -113,17 +134,6 @@ k_p1_tasks(const int* __restrict__ col_begin, const int* __restrict__ deg, int c
     }
 }
 
-// tab[p] = exp(-2*pi*i*p/rows), p < ntab
-// two_level: entries TWO_LO.. hold W^(TWO_LO*j) (layout of TAB_TWO)
-__global__ void k_table_rows(float2* __restrict__ tab, int ntab, int rows, int two_level) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ntab) return;
-    const long long p = (two_level && i >= TWO_LO) ? (long long)(i - TWO_LO) * TWO_LO % rows : i;
-    double s, c;
-    sincospi(-2.0 * (double)p / (double)rows, &s, &c);
-    tab[i] = make_float2((float)c, (float)s);
-}
-
 // Chirp exp(-i*pi*c^2/cols) times W_L^{+c*q} (sign = +1) or W_L^{-c*q} (sign = -1),
 // W_L = exp(-2*pi*i/L); c^2 mod 2*cols and c*q mod L are reduced exactly.
 __device__ __forceinline__ float2 chirp_twiddle(long long c, int q, int cols, int L, int sign) {
@@ -135,38 +145,62 @@ __device__ __forceinline__ float2 chirp_twiddle(long long c, int q, int cols, in
     return make_float2((float)co, (float)s);
 }
 
-// pre[q][c] = W_L^{+c*q}  (channel pre-twiddle; the chirp is applied by pass 1)
-__global__ void k_table_pre(float2* __restrict__ pre, int cols, int L, int K) {
-    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)K * cols) return;
-    int q = (int)(idx / cols);
-    long long c = idx - (long)q * cols;
-    long long cq = (c * (long long)q) % (long long)L;
-    double s, co;
-    sincospi(-2.0 * (double)cq / (double)L, &s, &co);
-    pre[idx] = make_float2((float)co, (float)s);
-}
-
-// post[q][c] = chirp(c) * W_L^{-c*q}  (column order)
-__global__ void k_table_post(float2* __restrict__ post, int cols, int L, int K) {
-    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)K * cols) return;
-    int q = (int)(idx / cols);
-    int c = (int)(idx - (long)q * cols);
-    post[idx] = chirp_twiddle(c, q, cols, L, -1);
-}
-
-// Stage twiddles, q-major: tw[off + (q-1)*m + k] = W_{Lp}^{q*k*l}, l = Lp/(R*m).
-__global__ void k_table_fft(float2* __restrict__ tw, int Lp, int R, int m, int off) {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= m * (R - 1)) return;
-    int q = idx / m + 1;
-    int k = idx - (q - 1) * m;
-    long long l = Lp / (R * m);
-    long long e = ((long long)q * k * l) % Lp;
+// exp(-2*pi*i*e/n) for an exactly reduced integer phase e < n
+__device__ __forceinline__ float2 root_f32(long long e, long long n) {
     double s, c;
-    sincospi(-2.0 * (double)e / (double)Lp, &s, &c);
-    tw[off + idx] = make_float2((float)c, (float)s);
+    sincospi(-2.0 * (double)e / (double)n, &s, &c);
+    return make_float2((float)c, (float)s);
+}
+
+// The single-precision plan tables in one launch, one entry per thread over
+// the concatenated index ranges
+//   rowtab[p] = W_rows^p, p < ntab (two_level: entries TWO_LO.. hold
+//              W_rows^(TWO_LO*j), the layout of TAB_TWO)
+//   pre[q][c] = W_L^{+c*q}              (channel pre-twiddle)
+//   post[q][c] = chirp(c) * W_L^{-c*q}  (column order)
+//   fftw: stage s's twiddles, q-major, tw[twoff[s] + (q-1)*m + k] =
+//         W_Lp^{q*k*l}, l = Lp/(R*m)
+struct TableArgs {
+    float2* rowtab;
+    float2* pre;
+    float2* post;
+    float2* fftw;
+    int ntab, rows, two_level, cols, L, K;
+    FFTDesc fd;
+};
+__global__ void k_tables(TableArgs a) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.ntab) {
+        const long long p = (a.two_level && i >= TWO_LO) ? (long long)(i - TWO_LO) * TWO_LO % a.rows : i;
+        a.rowtab[i] = root_f32(p, a.rows);
+        return;
+    }
+    i -= a.ntab;
+    const long kc = (long)a.K * a.cols;
+    if (i < 2 * kc) {
+        const bool post = i >= kc;
+        const long idx = post ? i - kc : i;
+        const int q = (int)(idx / a.cols);
+        const long long c = idx - (long)q * a.cols;
+        if (post)
+            a.post[idx] = chirp_twiddle(c, q, a.cols, a.L, -1);
+        else
+            a.pre[idx] = root_f32((c * (long long)q) % (long long)a.L, a.L);
+        return;
+    }
+    i -= 2 * kc;
+    for (int s = 0; s < a.fd.nst; s++) {
+        const int R = a.fd.R[s], m = a.fd.m[s];
+        const long n = (long)(R - 1) * m;
+        if (i < n) {
+            const int q = (int)(i / m) + 1;
+            const int k = (int)(i - (long)(q - 1) * m);
+            const long long l = a.fd.Lp / (R * m);
+            a.fftw[a.fd.twoff[s] + i] = root_f32(((long long)q * k * l) % a.fd.Lp, a.fd.Lp);
+            return;
+        }
+        i -= n;
+    }
 }
 
 // Channel-q filter input: bq[q][n] = sum_{c = n mod Lp, c < L} b[c] * W_L^{c*q}
