@@ -253,8 +253,23 @@ __global__ void k_dif_stage_f64(const double2* __restrict__ src, double2* __rest
     const int span = R * m;
     const int j = pos / span, rem = pos - j * span, q = rem / m, k = rem - q * m;
     const double2* x = src + (size_t)ch * Lp + (size_t)j * span + k;
+    // inputs in groups of 8 loads issued together (R is a runtime value: a
+    // load-multiply chain would pay the L2 latency R times); sum order s = 0..R-1
     double2 acc = make_double2(0.0, 0.0);
-    for (int s = 0, e = 0; s < R; s++, e = (e + q) % R) acc = cadd(acc, cmul(x[(size_t)s * m], root[e]));
+    int e = 0;
+    for (int s0 = 0; s0 < R; s0 += 8) {
+        double2 xv[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) xv[i] = (s0 + i < R) ? x[(size_t)(s0 + i) * m] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (s0 + i < R) {
+                acc = cadd(acc, cmul(xv[i], root[e]));
+                e += q;
+                if (e >= R) e -= R;
+            }
+        }
+    }
     const long long l = Lp / span;
     const long long ph = ((long long)q * k * l) % Lp;
     double sn, cs;
