@@ -20,6 +20,7 @@ GBSP_ERR_ALLOC = 3
 GBSP_ERR_UNSUPPORTED = 4
 GBSP_ERR_IO = 5
 GBSP_ERR_NOT_BUILT = 6
+GBSP_LEN_POW2 = 2
 GBSP_LEN_3SMOOTH = 3
 GBSP_LEN_7SMOOTH = 7
 GBSP_PLANNER_MODEL = 0

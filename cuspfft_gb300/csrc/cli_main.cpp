@@ -102,14 +102,17 @@ void usage(const char* prog) {
             "  --csc-mixed-radix  Binary CSC + Bluestein, fft_len next 3-smooth (sm_103a kernels)\n"
             "  --csc-mixed-radix-graph  Same, replayed as one CUDA graph\n"
             "  --csc-cufft-smooth  Binary CSC + Bluestein, fft_len next 7-smooth (own kernels, no cuFFT)\n"
-            "  --csc-stockham-stream  Streaming variant: tiles copied to pinned host memory (3-smooth)\n"
-            "  --csc-stockham-cufft-stream  Streaming variant, 7-smooth length (own kernels, no cuFFT)\n"
+            "  --csc-stockham-smem  Binary CSC + Bluestein, fft_len next power of two\n"
+            "  --csc-stockham-cufft  Same length (own kernels, no cuFFT)\n"
+            "  --csc-stockham-stream  Streaming variant: tiles copied to pinned host memory (power of two)\n"
+            "  --csc-stockham-cufft-stream  Streaming variant, power-of-two length (own kernels, no cuFFT)\n"
+            "  --csc-binary-lut  Streaming, power-of-two length (pass 1: exact twiddle table)\n"
+            "  --csc-binary-stockham-smem  Non-streaming, power-of-two length (same pass 1)\n"
             "  --csc-tile N     Bluestein rows per tile (default: 1024)\n"
             "  --cpu-reference  Host FP64 reference spectrum; every method is checked against it\n"
             "  --repeat N       1 warm-up + N timed runs; report median, min, max (default 1)\n"
-            "  (--csc-bluestein --csc-stockham --csc-stockham-smem --csc-stockham-cufft\n"
-            "   --csc-stockham-graph --spfft --csc-binary-lut --csc-binary-stockham-smem are\n"
-            "   accepted and report 'not in this build')\n",
+            "  (--csc-bluestein --csc-stockham --csc-stockham-graph, which select nothing in the\n"
+            "   reference CLI, and --spfft are accepted and report 'not in this build')\n",
             prog);
 }
 
@@ -122,6 +125,7 @@ int main(int argc, char** argv) {
 
     bool run_dense = true, run_sparse = true;
     bool mixed = false, mixed_graph = false, smooth = false, cpu_ref = false, stream3 = false, stream7 = false;
+    bool stk_smem = false, stk_cufft = false, bin_lut = false, bin_smem = false;
     std::vector<std::string> unbuilt;
     int tile = 1024, repeat = 1;
     try {
@@ -135,14 +139,17 @@ int main(int argc, char** argv) {
             else if (f == "--cpu-reference") cpu_ref = true;
             else if (f == "--csc-stockham-stream") stream3 = true;
             else if (f == "--csc-stockham-cufft-stream") stream7 = true;
+            else if (f == "--csc-stockham-smem") stk_smem = true;
+            else if (f == "--csc-stockham-cufft") stk_cufft = true;
+            else if (f == "--csc-binary-lut") bin_lut = true;
+            else if (f == "--csc-binary-stockham-smem") bin_smem = true;
             else if (f == "--csc-tile" || f == "--repeat") {
                 if (++i >= argc) throw std::runtime_error(f + " requires an integer value");
                 int v = std::stoi(argv[i]);
                 if (v <= 0) throw std::runtime_error(f + " must be positive");
                 (f == "--csc-tile" ? tile : repeat) = v;
-            } else if (f == "--csc-bluestein" || f == "--csc-stockham" || f == "--csc-stockham-smem" ||
-                       f == "--csc-stockham-cufft" || f == "--csc-stockham-graph" ||
-                       f == "--spfft" || f == "--csc-binary-lut" || f == "--csc-binary-stockham-smem") {
+            } else if (f == "--csc-bluestein" || f == "--csc-stockham" || f == "--csc-stockham-graph" ||
+                       f == "--spfft") {
                 unbuilt.push_back(f);
             } else {
                 throw std::runtime_error("Unknown option: " + f);
@@ -177,17 +184,26 @@ int main(int argc, char** argv) {
         if (run_dense) print_fail("Dense cuFFT (baseline)", "not in this build");
 
         struct M { bool on; const char* label; const char* check; std::function<SparseFFTResult()> fn; };
+        // rows in the reference CLI's order (src/main.cu:480-700)
         std::vector<M> methods = {
             {mixed, "Sparse CSC (mixed-radix)", "Sparse CSC mixed-radix",
              [&] { return sparse_fft_csc_bluestein_mixed_radix(coo, tile); }},
             {smooth, "Sparse CSC (cufft smooth)", "Sparse CSC cufft smooth",
              [&] { return sparse_fft_csc_bluestein_cufft_smooth(coo, tile); }},
-            {mixed_graph, "Sparse CSC (mr-graph)", "Sparse CSC mr-graph",
-             [&] { return sparse_fft_csc_bluestein_mixed_radix_graph(coo, tile); }},
+            {stk_smem, "Sparse CSC (Stk smem)", "Sparse CSC Stk smem",
+             [&] { return sparse_fft_csc_bluestein_smem(coo, tile); }},
+            {stk_cufft, "Sparse CSC (Bluestein+cufft)", "Sparse CSC Bluestein+cufft",
+             [&] { return sparse_fft_csc_bluestein_cufft(coo, tile); }},
             {stream3, "Sparse CSC (Stockham strm)", "Sparse CSC Stockham strm",
              [&] { return sparse_fft_csc_stockham_streaming(coo, tile, 0); }},
             {stream7, "Sparse CSC (cufft stream)", "Sparse CSC cufft stream",
              [&] { return sparse_fft_csc_bluestein_cufft_streaming(coo, tile); }},
+            {bin_lut, "Sparse CSC (binary LUT)", "Sparse CSC binary LUT",
+             [&] { return sparse_fft_csc_bluestein_binary_lut(coo, tile); }},
+            {mixed_graph, "Sparse CSC (mr-graph)", "Sparse CSC mr-graph",
+             [&] { return sparse_fft_csc_bluestein_mixed_radix_graph(coo, tile); }},
+            {bin_smem, "Sparse CSC (binary Stk smem)", "Sparse CSC binary Stk smem",
+             [&] { return sparse_fft_csc_stockham_binary_smem(coo, tile); }},
         };
         for (auto& m : methods) {
             if (!run_sparse || !m.on) continue;

@@ -25,6 +25,11 @@ int set_error(int status, const std::string& msg) {
 
 long next_smooth(long n, int policy) {
     if (n < 1) n = 1;
+    if (policy == GBSP_LEN_POW2) {
+        long p = 1;
+        while (p < n) p <<= 1;
+        return p;
+    }
     static const int p3[] = {2, 3};
     static const int p7[] = {2, 3, 5, 7};
     const int* ps = (policy == GBSP_LEN_7SMOOTH) ? p7 : p3;
@@ -67,7 +72,7 @@ int gbsp_last_error(char* buf, size_t buflen) {
 }
 
 int gbsp_next_smooth(int n, int policy) {
-    if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH) return -1;
+    if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH && policy != GBSP_LEN_POW2) return -1;
     long m = gbsp::next_smooth(n, policy);
     return m > 0x7fffffffL ? -1 : (int)m;
 }

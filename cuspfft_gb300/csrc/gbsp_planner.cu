@@ -150,8 +150,8 @@ std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_op
 
 int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSplit* out) {
     const int policy = (o && o->length_policy) ? o->length_policy : GBSP_LEN_3SMOOTH;
-    if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH)
-        return set_error(GBSP_ERR_INVALID, "length_policy must be 3 or 7");
+    if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH && policy != GBSP_LEN_POW2)
+        return set_error(GBSP_ERR_INVALID, "length_policy must be 2, 3 or 7");
     const int nt_opt = o ? o->rows_threads : 0;
     if (nt_opt < 0 || nt_opt % 32 || nt_opt > 1024)
         return set_error(GBSP_ERR_INVALID, "rows_threads must be 0 or a multiple of 32 up to 1024");

@@ -187,10 +187,6 @@ SparseFFTResult run_streaming(const COOMatrix& coo, int u_tile, int policy) {
     return r;
 }
 
-[[noreturn]] void not_built(const char* name) {
-    throw std::runtime_error(std::string(name) + ": not in this build");
-}
-
 }  // namespace
 
 // ---- mtx_reader.h ----------------------------------------------------------
@@ -248,30 +244,34 @@ SparseFFTResult sparse_fft_csc_bluestein_cufft_smooth(const COOMatrix& coo, int 
     return run_method(coo, u_tile, GBSP_LEN_7SMOOTH);
 }
 
-SparseFFTResult sparse_fft_csc_bluestein(const COOMatrix&, int, bool, int) {
-    not_built("sparse_fft_csc_bluestein");
+// The reference's power-of-two methods (fft_len = next_power_of_two(2 cols - 1),
+// src/sparse_fft_bluestein.cu:687, 918, 1160, 1500, 1767).  use_stockham and
+// fft_backend only pick the reference's FFT implementation (Stockham loop,
+// shared-memory Stockham, cuFFT); the byte-mask LUT methods differ from it
+// only in how pass 1 forms the twiddle sums.  Every one computes the same
+// spectrum, here with the sm_103a kernels at the method's own length.
+SparseFFTResult sparse_fft_csc_bluestein(const COOMatrix& coo, int u_tile, bool, int) {
+    return run_method(coo, u_tile, GBSP_LEN_POW2);
 }
-SparseFFTResult sparse_fft_csc_bluestein_smem(const COOMatrix&, int) {
-    not_built("sparse_fft_csc_bluestein_smem");
+SparseFFTResult sparse_fft_csc_bluestein_smem(const COOMatrix& coo, int u_tile) {
+    return run_method(coo, u_tile, GBSP_LEN_POW2);
 }
-SparseFFTResult sparse_fft_csc_bluestein_cufft(const COOMatrix&, int) {
-    not_built("sparse_fft_csc_bluestein_cufft");
+SparseFFTResult sparse_fft_csc_bluestein_cufft(const COOMatrix& coo, int u_tile) {
+    return run_method(coo, u_tile, GBSP_LEN_POW2);
 }
-// Streaming methods: same transform as the two hot methods, output to host.
-// fft_backend only selects the FFT library in the reference; here every
-// backend runs the sm_103a kernels (3-smooth length).
+// Streaming methods: output to pinned host memory, returned in h_output.
 SparseFFTResult sparse_fft_csc_stockham_streaming(const COOMatrix& coo, int u_tile, int) {
-    return run_streaming(coo, u_tile, GBSP_LEN_3SMOOTH);
+    return run_streaming(coo, u_tile, GBSP_LEN_POW2);
 }
 SparseFFTResult sparse_fft_csc_bluestein_cufft_streaming(const COOMatrix& coo, int u_tile) {
-    return run_streaming(coo, u_tile, GBSP_LEN_7SMOOTH);
+    return run_streaming(coo, u_tile, GBSP_LEN_POW2);
 }
-SparseFFTResult sparse_fft_csc_stockham_graph(const COOMatrix&, int) {
-    not_built("sparse_fft_csc_stockham_graph");
+SparseFFTResult sparse_fft_csc_stockham_graph(const COOMatrix& coo, int u_tile) {
+    return run_streaming(coo, u_tile, GBSP_LEN_POW2);
 }
-SparseFFTResult sparse_fft_csc_bluestein_binary_lut(const COOMatrix&, int) {
-    not_built("sparse_fft_csc_bluestein_binary_lut");
+SparseFFTResult sparse_fft_csc_bluestein_binary_lut(const COOMatrix& coo, int u_tile) {
+    return run_streaming(coo, u_tile, GBSP_LEN_POW2);
 }
-SparseFFTResult sparse_fft_csc_stockham_binary_smem(const COOMatrix&, int) {
-    not_built("sparse_fft_csc_stockham_binary_smem");
+SparseFFTResult sparse_fft_csc_stockham_binary_smem(const COOMatrix& coo, int u_tile) {
+    return run_method(coo, u_tile, GBSP_LEN_POW2);
 }

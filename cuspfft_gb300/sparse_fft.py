@@ -14,8 +14,8 @@ from typing import Optional
 import numpy as np
 
 from . import _capi
-from ._capi import (GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GBSP_PLANNER_LEARNED, GBSP_PLANNER_MODEL, GbspMatrix,
-                    GbspOptions, GbspPlanInfo, check, load)
+from ._capi import (GBSP_LEN_3SMOOTH, GBSP_LEN_7SMOOTH, GBSP_LEN_POW2, GBSP_PLANNER_LEARNED, GBSP_PLANNER_MODEL,
+                    GbspMatrix, GbspOptions, GbspPlanInfo, check, load)
 
 
 @dataclass
@@ -355,3 +355,27 @@ def sparse_fft_csc_bluestein_cufft_smooth(coo: COOMatrix, u_tile: int = 128) -> 
     """Reference include/sparse_fft.h:70 -- fft_len = next 7-smooth >= 2*cols-1,
     computed by this library's own FFT (no cuFFT)."""
     return _run_method(coo, u_tile, GBSP_LEN_7SMOOTH)
+
+
+def sparse_fft_csc_bluestein(coo: COOMatrix, u_tile: int = 256, use_stockham: bool = False,
+                             fft_backend: int = 0) -> SparseFFTResult:
+    """Reference include/sparse_fft.h:23 -- fft_len = next power of two >=
+    2*cols-1.  use_stockham and fft_backend pick the reference's FFT
+    implementation; here every backend runs this library's kernels."""
+    return _run_method(coo, u_tile, GBSP_LEN_POW2)
+
+
+def sparse_fft_csc_bluestein_smem(coo: COOMatrix, u_tile: int = 256) -> SparseFFTResult:
+    """Reference include/sparse_fft.h:26 (fft_backend 1 of the above)."""
+    return _run_method(coo, u_tile, GBSP_LEN_POW2)
+
+
+def sparse_fft_csc_bluestein_cufft(coo: COOMatrix, u_tile: int = 256) -> SparseFFTResult:
+    """Reference include/sparse_fft.h:27 (fft_backend 3; no cuFFT here)."""
+    return _run_method(coo, u_tile, GBSP_LEN_POW2)
+
+
+def sparse_fft_csc_stockham_binary_smem(coo: COOMatrix, u_tile: int = 128) -> SparseFFTResult:
+    """Reference include/sparse_fft.h:83 -- power-of-two length, non-streaming;
+    the byte-mask LUT pass 1 is replaced by this library's pass 1 (same sums)."""
+    return _run_method(coo, u_tile, GBSP_LEN_POW2)

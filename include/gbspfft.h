@@ -42,7 +42,11 @@ enum {
  *   GBSP_LEN_7SMOOTH: fft_len = next 2^a*3^b*5^c*7^d >= 2*cols-1
  *                     (reference: next_7_smooth, :1987-1994,
  *                      used by sparse_fft_csc_bluestein_cufft_smooth) */
-enum { GBSP_LEN_3SMOOTH = 3, GBSP_LEN_7SMOOTH = 7 };
+/*   GBSP_LEN_POW2:    fft_len = next power of two >= 2*cols-1
+ *                     (reference: next_power_of_two, include/sparse_fft_internal.cuh:153-157,
+ *                      used by sparse_fft_csc_bluestein and its _smem / _cufft wrappers,
+ *                      the streaming, graph and binary-LUT methods) */
+enum { GBSP_LEN_POW2 = 2, GBSP_LEN_3SMOOTH = 3, GBSP_LEN_7SMOOTH = 7 };
 
 /* How a plan picks its radices, row block and pass-1 shape when the options
  * leave them open.
@@ -71,7 +75,7 @@ typedef struct gbsp_plan_s* gbsp_plan_t;
 /* Tuning knobs.  Zero-initialise and set what you need; 0 means "default".
  * None of them changes the computed spectrum beyond FP32 rounding. */
 typedef struct {
-    int length_policy;     /* GBSP_LEN_3SMOOTH (default) or GBSP_LEN_7SMOOTH            */
+    int length_policy;     /* GBSP_LEN_3SMOOTH (default), GBSP_LEN_7SMOOTH or GBSP_LEN_POW2 */
     int u_tile;            /* Bluestein rows per tile (each yields output rows u and
                               rows-u); the --csc-tile analogue. 0 = all rows in one tile */
     int kahan_min_degree;  /* columns with >= this many nonzeros accumulate with Kahan

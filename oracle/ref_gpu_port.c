@@ -11,7 +11,8 @@
  *   FFT      out-of-place Stockham stages (:184-215 radix 2, :2017-2080 radix 3;
  *            the radix-9 stage :2093-2209 is two radix-3 stages fused, run here
  *            as the two stages) with twiddle angles formed in float; the
- *            7-smooth method's cuFFT (:2605-2686) is replaced by the same
+ *            7-smooth method's cuFFT (:2605-2686) and the power-of-two
+ *            methods' FFTs are replaced by the same
  *            Stockham engine with radix 5 and 7 stages (cuFFT is closed
  *            source; only its contract -- an FP32 C2C FFT -- is restated).
  *   filter   B = FFT(b), b from make_bluestein_b (include/sparse_fft_internal.cuh:179-191)
@@ -139,12 +140,19 @@ static cf* fft_row(cf* a, cf* b, int n, const stage_t* st, int nr, int inverse) 
 /*
  * Full transform.  csc arrays as make_compact_csc returns them; out is
  * rows x (cols/2+1) interleaved float pairs.  method: 3 = mixed-radix
- * (3-smooth), 7 = cufft-smooth (7-smooth).  Returns 0 on success.
+ * (3-smooth), 7 = cufft-smooth (7-smooth), 2 = the power-of-two methods
+ * (sparse_fft_csc_bluestein and the others at
+ * fft_len = next_power_of_two(2*cols-1), include/sparse_fft_internal.cuh:153-157,
+ * radix-2 stages).  Returns 0 on success.
  */
 int port_sparse_fft(int rows, int cols, int n_active, const int* sparse_cols, const int* col_ptr,
                     const int* row_idx, int method, float* out) {
     const int seven = (method == 7);
-    const int L = next_smooth(2 * cols - 1, seven);
+    int L = 1;
+    if (method == 2)
+        while (L < 2 * cols - 1) L <<= 1;
+    else
+        L = next_smooth(2 * cols - 1, seven);
     int rs[64];
     const int nr = radix_list(L, seven, rs);
     if (nr < 0) return 1;

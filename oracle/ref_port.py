@@ -132,6 +132,14 @@ def can_pack_u16(rows: int, cols: int) -> bool:
     return rows <= 65536 and cols <= 65536
 
 
+def next_power_of_two(n: int) -> int:
+    """include/sparse_fft_internal.cuh:153-157"""
+    p = 1
+    while p < n:
+        p <<= 1
+    return p
+
+
 def next_smooth(n: int, seven: bool) -> int:
     """src/sparse_fft_bluestein.cu:1975-1994"""
     m = n
@@ -207,8 +215,9 @@ def _port_lib():
 
 def reference_gpu_method(rows: int, cols: int, row_idx, col_idx, method: int) -> np.ndarray:
     """rows x (cols/2+1) complex64 spectrum from the FP32 CPU restatement of
-    sparse_fft_csc_bluestein_mixed_radix (method 3) or
-    sparse_fft_csc_bluestein_cufft_smooth (method 7)."""
+    sparse_fft_csc_bluestein_mixed_radix (method 3),
+    sparse_fft_csc_bluestein_cufft_smooth (method 7) or the power-of-two
+    methods (method 2: sparse_fft_csc_bluestein and its wrappers)."""
     sc, cp, ri = make_compact_csc(rows, cols, row_idx, col_idx)
     sc, cp = np.ascontiguousarray(sc, np.int32), np.ascontiguousarray(cp, np.int32)
     ri = np.ascontiguousarray(ri if ri.size else np.zeros(1, np.int32), np.int32)

@@ -12,6 +12,7 @@
 //   make_bluestein_chirp / _b   include/sparse_fft_internal.cuh:168-191
 //   next_3_smooth / next_7_smooth / factor_3_smooth
 //                               src/sparse_fft_bluestein.cu:1975-2011
+//   next_power_of_two           include/sparse_fft_internal.cuh:153-157
 #include <cstdlib>
 #include <cstring>
 #include <stdexcept>
@@ -82,6 +83,7 @@ void ref_bluestein_b(int n, int fft_len, float* out) {
 
 int ref_next_3_smooth(int n) { return next_3_smooth(n); }
 int ref_next_7_smooth(int n) { return next_7_smooth(n); }
+int ref_next_power_of_two(int n) { return next_power_of_two(n); }
 
 int ref_factor_3_smooth(int n, int* out, int cap) {
     try {

@@ -34,6 +34,7 @@ def lib():
         _lib.ref_bluestein_b.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float)]
         _lib.ref_next_3_smooth.argtypes = [C.c_int]
         _lib.ref_next_7_smooth.argtypes = [C.c_int]
+        _lib.ref_next_power_of_two.argtypes = [C.c_int]
         _lib.ref_factor_3_smooth.argtypes = [C.c_int, ip, C.c_int]
     return _lib
 
@@ -88,6 +89,10 @@ def next_3_smooth(n: int) -> int:
 
 def next_7_smooth(n: int) -> int:
     return lib().ref_next_7_smooth(n)
+
+
+def next_power_of_two(n: int) -> int:
+    return lib().ref_next_power_of_two(n)
 
 
 def factor_3_smooth(n: int) -> list:

@@ -60,6 +60,13 @@ def test_smooth_lengths():
         assert ref_port.next_smooth(int(n), True) == s7
 
 
+def test_power_of_two_lengths():
+    # the reference's pow2 methods: fft_len = next_power_of_two(2*cols - 1)
+    assert gb.next_smooth(2 * 8219 - 1, gb.GBSP_LEN_POW2) == 32768
+    for n in list(range(1, 5000)) + [65535, 65536, 65537, 80841, (1 << 27) + 1]:
+        assert gb.next_smooth(n, gb.GBSP_LEN_POW2) == ref_port.next_power_of_two(n)
+
+
 def test_factor_3_smooth():
     for k in TABLES.files:
         if k.startswith("factor3/"):
@@ -105,3 +112,4 @@ def test_live_reference_host_code():
     for n in g.integers(1, 100000, 50):
         assert gb.next_smooth(int(n), 3) == refhost.next_3_smooth(int(n))
         assert gb.next_smooth(int(n), 7) == refhost.next_7_smooth(int(n))
+        assert gb.next_smooth(int(n), gb.GBSP_LEN_POW2) == refhost.next_power_of_two(int(n))

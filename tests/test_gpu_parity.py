@@ -45,7 +45,7 @@ SHAPES = [(1, 1), (1, 7), (7, 1), (2, 2), (3, 5), (17, 31), (64, 64), (101, 97),
 
 
 @pytest.mark.parametrize("rows,cols", SHAPES)
-@pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH])
+@pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH, gb.GBSP_LEN_POW2])
 def test_random_shapes(cuda, rows, cols, policy):
     g = np.random.default_rng(rows * 1000 + cols)
     n = max(1, int(0.05 * rows * cols))
@@ -197,7 +197,9 @@ def test_reference_api_methods(cuda):
     import torch
     coo = synthetic.uniform_matrix(301, 127, 1500, seed=21)
     ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx)
-    for fn in (gb.sparse_fft_csc_bluestein_mixed_radix, gb.sparse_fft_csc_bluestein_cufft_smooth):
+    for fn in (gb.sparse_fft_csc_bluestein_mixed_radix, gb.sparse_fft_csc_bluestein_cufft_smooth,
+               gb.sparse_fft_csc_bluestein, gb.sparse_fft_csc_bluestein_smem, gb.sparse_fft_csc_bluestein_cufft,
+               gb.sparse_fft_csc_stockham_binary_smem):
         res = fn(coo, 16)
         assert res.output_cols == (coo.cols // 2 + 1 + 3) // 4 * 4
         assert res.ms > 0
@@ -207,7 +209,7 @@ def test_reference_api_methods(cuda):
         gb.sparse_fft_csc_bluestein_mixed_radix(coo, 0)
 
 
-@pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH])
+@pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH, gb.GBSP_LEN_POW2])
 @pytest.mark.parametrize("shape", [(64, 64, 400), (101, 127, 900), (300, 257, 3000), (211, 1000, 4000)])
 def test_against_reference_gpu_method_port(cuda, policy, shape):
     # the FP32 restatement of the reference's own method on the same input:
@@ -231,7 +233,8 @@ def test_uniform_3001x2048_vs_reference_port(cuda):
 
 def test_cli_methods_with_host_reference(cuda, tmp_path):
     # the reference-compatible driver end to end: read .mtx, run both hot
-    # methods and the graph replay, check lines against the FP64 host spectrum
+    # methods, the graph replay and the power-of-two methods (direct and
+    # streamed), check lines against the FP64 host spectrum
     import subprocess
     from cuspfft_gb300 import build
     coo = synthetic.uniform_matrix(97, 130, 900, seed=31)
@@ -243,11 +246,13 @@ def test_cli_methods_with_host_reference(cuda, tmp_path):
             f.write(f"{r + 1} {c + 1}\n")
     exe = build.build().parent / "cuspfft_gb300"
     res = subprocess.run([str(exe), str(path), "--sparse-only", "--cpu-reference", "--csc-mixed-radix",
-                          "--csc-cufft-smooth", "--csc-mixed-radix-graph", "--csc-tile", "16", "--repeat", "3"],
+                          "--csc-cufft-smooth", "--csc-mixed-radix-graph", "--csc-stockham-smem",
+                          "--csc-stockham-cufft", "--csc-stockham-cufft-stream", "--csc-binary-lut",
+                          "--csc-binary-stockham-smem", "--csc-tile", "16", "--repeat", "3"],
                          capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr
     checks = [ln for ln in res.stdout.splitlines() if ln.strip().startswith("check")]
-    assert len(checks) == 3, res.stdout
+    assert len(checks) == 8, res.stdout
     for ln in checks:
         max_rel = float(ln.split("max_rel")[1].split()[0])
         assert max_rel < 1e-4, ln
