@@ -144,11 +144,15 @@ int helper_stream(int dev, cudaStream_t* hs) {
 void free_plan(gbsp_plan_s* p) {
     if (!p) return;
     if (p->arena && p->arena_pooled) {
-        // the plan's kernels may run on any stream: wait for the device, as
-        // cudaFree would, before the arena goes back to the pool
+        // the plan's kernels may run on any stream: wait for the plan's
+        // device, as cudaFree would, before the arena goes back to its pool
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (cur != p->device) cudaSetDevice(p->device);
         cudaDeviceSynchronize();
         cudaFreeAsync(p->arena, 0);
         cudaStreamSynchronize(0);
+        if (cur >= 0 && cur != p->device) cudaSetDevice(cur);
     }
     for (void* a : p->allocs) cudaFree(a);
     for (int b = 0; b < 2; b++) {
