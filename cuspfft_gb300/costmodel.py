@@ -4,7 +4,7 @@ can be chosen without measuring (planner="learned").
 
 Everything numeric runs in the library's hand-written kernels
 (gbsp_mlp_forward / gbsp_mlp_backward / gbsp_mlp_adam); torch only provides
-device memory.  The exhaustive autotuner stays the fallback and the judge of
+device memory.  The exhaustive autotuner stays the fallback and the arbiter of
 the model's regret.  The spectrum never depends on the model.
 
 Dataset (one row per matrix, padded to 8 row choices x 6 pass-1 shapes):

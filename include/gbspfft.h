@@ -175,7 +175,7 @@ int gbsp_plan_destroy(gbsp_plan_t plan);
 /* Freed plan memory the library's pool keeps for later plans, per device
  * (default 1 GiB): a cudaMalloc and a cudaFree of a plan's allocation cost
  * ~0.1 ms each, a pooled one a few microseconds.  Memory above the limit
- * goes back to the driver at the next synchronisation; 0 keeps nothing.
+ * goes back to the CUDA driver at the next synchronisation; 0 keeps nothing.
  * Takes effect at once (trims the pools to the new limit). */
 int gbsp_set_memory_cache(size_t bytes);
 
