@@ -223,10 +223,14 @@ struct P1Args {
     int cw, cols, s_cols, ntab, rows, u0, tile_rows, kahan_min;
     uint32_t magic;
     unsigned long long magic64;  // ceil(2^64 / rows), for rows > 65535
+    // k_twiddle_sum's item queue: [0] next item, [1] CTAs done; zero before
+    // the first launch, and the last CTA of each launch zeroes it again
+    unsigned int* queue;
 };
 
 struct P1Shared {
     int next_task;
+    unsigned int item;
     int slot0[64 + 1];
     float2 chirp[64];
 };
@@ -312,10 +316,27 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
     float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
     for (int i = threadIdx.x; i < a.ntab; i += blockDim.x) tab[i] = a.row_tab[i];
     if (threadIdx.x == 0) sh.next_task = 0;
-    __syncthreads();
+    // Items are handed out one at a time from a device counter, so CTAs
+    // whose windows hold fewer nonzeros take more items and all finish
+    // together.  p1_item ends on a barrier, so thread 0 rewrites sh.item only
+    // after every thread has read it.
     const long nitems = p1_items(a, 32 * KU);
-    for (long it = blockIdx.x; it < nitems; it += gridDim.x)
+    for (;;) {
+        if (threadIdx.x == 0) sh.item = atomicAdd(&a.queue[0], 1u);
+        __syncthreads();
+        const long it = sh.item;
+        if (it >= nitems) break;
         p1_item<IDX, TAB, BIG, KU>(a, it, stage, info_all, tab, sh);
+    }
+    // the last CTA out (every other one has stopped taking items) rearms the
+    // queue for the next launch
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&a.queue[1], 1u) == gridDim.x - 1) {
+            atomicExch(&a.queue[0], 0u);
+            atomicExch(&a.queue[1], 0u);
+        }
+    }
 }
 
 // Batched pass 1: the work items of many matrices (item_begin: first item of

@@ -199,6 +199,7 @@ gbsp::P1Args p1_args(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pi
     a.kahan_min = p->kahan_min;
     a.magic = p->rows_magic;
     a.magic64 = p->rows_magic64;
+    a.queue = reinterpret_cast<unsigned int*>(p->d_err + 2);
     return a;
 }
 
@@ -423,7 +424,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     const int K = p->K, Lp = p->Lp, cols = p->cols;
     const int ntw = std::max(fft_tw_count(p->fd), 1);
     {
-        const size_t sizes[] = {tbl_bytes, (size_t)std::max(p->nnz, 1) * p->idx_bytes, 2 * sizeof(int),
+        const size_t sizes[] = {tbl_bytes, (size_t)std::max(p->nnz, 1) * p->idx_bytes, 4 * sizeof(int),
                                 (size_t)p->ntab * sizeof(float2), (size_t)K * cols * sizeof(float2),
                                 (size_t)K * cols * sizeof(float2), (size_t)K * Lp * sizeof(float2),
                                 (size_t)ntw * sizeof(float2), (size_t)K * Lp * sizeof(double2),
@@ -466,8 +467,9 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (K - 1) * Lp * sizeof(float2))))
         return rc;
     if ((rc = dev_alloc(p, &p->d_row_idx, (size_t)std::max(p->nnz, 1) * p->idx_bytes))) return rc;
-    // [1]: plan-build checks (bit 0 a row index out of range, bit 1 a task overflow)
-    if ((rc = dev_alloc(p, (void**)&p->d_err, 2 * sizeof(int)))) return rc;
+    // [1]: plan-build checks (bit 0 a row index out of range, bit 1 a task
+    // overflow); [2], [3]: pass 1's item queue
+    if ((rc = dev_alloc(p, (void**)&p->d_err, 4 * sizeof(int)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_S, s_bytes))) return rc;
     char* d_stage = reinterpret_cast<char*>(p->d_S);
     if (staging > 0 && (rc = dev_alloc(p, (void**)&d_stage, staging))) return rc;
@@ -542,7 +544,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     int* d_cp = reinterpret_cast<int*>(d_stage + st_row);
     int* d_sc = reinterpret_cast<int*>(d_stage + st_row + st_cp);
     int* d_in = (p->idx_bytes == 2) ? reinterpret_cast<int*>(d_stage) : static_cast<int*>(p->d_row_idx);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p->d_err, 0, 2 * sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->d_err, 0, 4 * sizeof(int), st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_cp, col_ptr, (size_t)(na + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && na > 0)
