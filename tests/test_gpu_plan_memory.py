@@ -53,3 +53,19 @@ def test_overlapping_plans(cuda):
     assert np.array_equal(spectrum(pc), want_a)
     pb.close()
     pc.close()
+
+
+def test_pass1_item_queue_rearms(cuda):
+    # pass 1 hands out work items from a device counter that the last CTA of
+    # each launch zeroes again: repeated and interleaved launches of two
+    # plans (whole transforms, tiles, pass 1 alone) must all see a fresh queue
+    import torch
+    a = synthetic.uniform_matrix(900, 700, 12000, seed=6)
+    b = synthetic.uniform_matrix(333, 1500, 8000, seed=7)
+    with gb.Plan(a) as pa, gb.Plan(b, u_tile=40) as pb:
+        want_a, want_b = spectrum(pa), spectrum(pb)
+        for _ in range(3):
+            s = torch.zeros((50, 704), dtype=torch.complex64, device="cuda")
+            pa.column_sums(10, 50, s)
+            assert np.array_equal(spectrum(pb), want_b)
+            assert np.array_equal(spectrum(pa), want_a)
