@@ -107,10 +107,13 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 //
 // Per nonzero r the lane reduces its phase (u*r) mod rows exactly with an
 // integer multiply-high and reads W_rows^p from the table staged in shared
-// memory.  The rows u + 32*kk in between reuse the exactly looked-up
-// W_rows^{(32*r) mod rows} as a complex multiplier, and every P1_RESEED rows
-// the value is looked up exactly again, so no twiddle is more than
-// P1_RESEED-1 products away from a correctly rounded table entry.  Sums of a
+// memory.  The rows u + 32*kk in between follow from the exactly looked-up
+// step z = W_rows^{(32*r) mod rows}: the first by one complex product, the
+// next ones by the three-term recurrence w[k+1] = 2cos(arg z)*w[k] - w[k-1]
+// (two FMAs instead of a four-operation product; its rounding error grows at
+// most linearly in the steps taken).  Every P1_RESEED rows the value is
+// looked up exactly again, so no twiddle is more than P1_RESEED-1 steps away
+// from a correctly rounded table entry.  Sums of a
 // batch of 32 nonzeros are added to the task total; for tasks of at least
 // kahan_min nonzeros that addition is Kahan-compensated.  The window's
 // results (times chirp[c] when a chirp table is given) leave as whole
@@ -169,8 +172,9 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
         for (int i = 0; i < cnt; i++) {
             const NzInfo z = info[i];  // one broadcast 16-byte load
             const float2 wd = make_float2(z.wx, z.wy);
+            const float c2 = 2.f * z.wx;  // 2cos(arg z), exact
             uint32_t p = mulmod_rows<BIG>(u_lane, z.r, rows, magic, magic64);
-            float2 w = make_float2(1.f, 0.f);
+            float2 w = make_float2(1.f, 0.f), wp = w;
 #pragma unroll
             for (int kk = 0; kk < KU; kk++) {
                 if (kk % P1_RESEED == 0) {
@@ -179,8 +183,13 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
                         const uint32_t pn = p + z.step;
                         p = min(pn, pn - rows);
                     }
-                } else {
+                } else if (kk % P1_RESEED == 1) {
+                    wp = w;
                     w = cmul(w, wd);
+                } else {
+                    const float2 wn = make_float2(fmaf(c2, w.x, -wp.x), fmaf(c2, w.y, -wp.y));
+                    wp = w;
+                    w = wn;
                 }
                 blk[kk].x += w.x;
                 blk[kk].y += w.y;
