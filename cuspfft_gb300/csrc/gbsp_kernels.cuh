@@ -288,8 +288,9 @@ __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage,
     }
     __syncthreads();
     const int ncol = min(cw, a.s_cols - c0);
+    const int cw_log2 = __ffs(cw) - 1;  // every pass-1 shape's window is 32 or 64 columns
     for (int e = threadIdx.x; e < UBLK * cw; e += blockDim.x) {
-        const int row = e / cw, lc = e - (e / cw) * cw;
+        const int row = e >> cw_log2, lc = e & (cw - 1);
         const int ul = ul0 + row;
         if (ul >= a.tile_rows || lc >= ncol) continue;
         const int p0 = sh.slot0[lc], p1 = sh.slot0[lc + 1];
