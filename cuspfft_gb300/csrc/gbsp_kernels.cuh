@@ -139,7 +139,7 @@ __device__ __forceinline__ float2 row_twiddle(const float2* tab, uint32_t p, uin
     return w;
 }
 
-// one nonzero as a warp shares it: row, reseed step, and W^{(32*r) mod rows}
+// one nonzero as a warp shares it: row, reseed step, and -W^{(32*r) mod rows}
 struct NzInfo {
     uint32_t r, step;
     float wx, wy;
@@ -162,40 +162,48 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
             const uint32_t d = mulmod_rows<BIG>(32u, r, rows, magic, magic64);
             const float2 wd = row_twiddle<TAB>(tab, d, rows, hr);
             const uint32_t st = (KU > P1_RESEED) ? mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic, magic64) : 0u;
-            info[lane] = NzInfo{r, st, wd.x, wd.y};
+            info[lane] = NzInfo{r, st, -wd.x, -wd.y};  // the step, negated
         }
         __syncwarp();
+        // Rows kk = 4g+1 and 4g+2 are carried negated, so every operation
+        // below is a plain packed FP32x2 add or FMA with no operand negation:
+        //   n1 = w0 * (-z)          = -w1
+        //   n2 = c2 * n1 + w0       = -(c2*w1 - w0) = -w2
+        //   w3 = (-c2) * n2 + n1    =   c2*w2 - w1
+        // Negation is exact and round-to-nearest is symmetric, so each value
+        // is bitwise the negative of the one the plain recurrence gives; the
+        // negated partial sums are flipped back after the batch.
+        static_assert(P1_RESEED == 4 && KU % 4 == 0, "pass-1 rows come in groups of four");
         float2 blk[KU];
 #pragma unroll
         for (int i = 0; i < KU; i++) blk[i] = make_float2(0.f, 0.f);
 #pragma unroll 4
         for (int i = 0; i < cnt; i++) {
             const NzInfo z = info[i];  // one broadcast 16-byte load
-            const float2 wd = make_float2(z.wx, z.wy);
-            const float c2 = 2.f * z.wx;  // 2cos(arg z), exact
+            const float2 nz = make_float2(z.wx, z.wy);
+            const float c2 = -2.f * z.wx;  // 2cos(arg z), exact
+            const float2 c2p = make_float2(c2, c2), mc2p = make_float2(-c2, -c2);
             uint32_t p = mulmod_rows<BIG>(u_lane, z.r, rows, magic, magic64);
-            float2 w = make_float2(1.f, 0.f), wp = w;
 #pragma unroll
-            for (int kk = 0; kk < KU; kk++) {
-                if (kk % P1_RESEED == 0) {
-                    w = row_twiddle<TAB>(tab, p, rows, hr);
-                    if (kk + P1_RESEED < KU) {
-                        const uint32_t pn = p + z.step;
-                        p = min(pn, pn - rows);
-                    }
-                } else if (kk % P1_RESEED == 1) {
-                    wp = w;
-                    w = cmul(w, wd);
-                } else {
-                    const float2 wn = make_float2(fmaf(c2, w.x, -wp.x), fmaf(c2, w.y, -wp.y));
-                    wp = w;
-                    w = wn;
+            for (int g = 0; g < KU; g += 4) {
+                const float2 w0 = row_twiddle<TAB>(tab, p, rows, hr);
+                if (g + 4 < KU) {
+                    const uint32_t pn = p + z.step;
+                    p = min(pn, pn - rows);
                 }
-                blk[kk].x += w.x;
-                blk[kk].y += w.y;
+                const float2 n1 = cmul(w0, nz);
+                const float2 n2 = __ffma2_rn(c2p, n1, w0);
+                const float2 w3 = __ffma2_rn(mc2p, n2, n1);
+                blk[g] = __fadd2_rn(blk[g], w0);
+                blk[g + 1] = __fadd2_rn(blk[g + 1], n1);
+                blk[g + 2] = __fadd2_rn(blk[g + 2], n2);
+                blk[g + 3] = __fadd2_rn(blk[g + 3], w3);
             }
         }
         __syncwarp();
+#pragma unroll
+        for (int kk = 0; kk < KU; kk++)
+            if (kk % 4 == 1 || kk % 4 == 2) blk[kk] = make_float2(-blk[kk].x, -blk[kk].y);
         if (compensated) {
 #pragma unroll
             for (int kk = 0; kk < KU; kk++) {
