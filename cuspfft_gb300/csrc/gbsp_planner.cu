@@ -182,7 +182,8 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
 
 // Preference order: 256-row items with 32-column windows, full table, then
 // half table; then 128-row items with 64- or 32-column windows; last the
-// two-level tables for matrices too tall for either.
+// two-level tables for matrices too tall for either.  Window widths must be
+// 32 or 64: the pass-1 window epilogue indexes its tile by shift and mask.
 const P1Shape kP1Shapes[N_P1_SHAPES] = {{8, 32, TAB_FULL}, {8, 32, TAB_HALF}, {4, 64, TAB_FULL}, {4, 32, TAB_FULL},
                                         {4, 64, TAB_HALF}, {4, 32, TAB_HALF}, {8, 32, TAB_TWO},  {4, 32, TAB_TWO}};
 
