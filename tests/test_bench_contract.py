@@ -1,0 +1,48 @@
+"""bench.py's output contract, checked on the CPU.
+
+- `--impl reference` times the reference's CPU path (its FFTW 2-D R2C,
+  restated with pocketfft) and prints one JSON line with the same metric,
+  unit and workload as the GPU arm, plus its cpu_baseline and e2e blocks.
+- The GPU arm has no CPU fallback: without a CUDA device it must exit
+  non-zero and print no result line.
+"""
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _run(*args, timeout=300):
+    return subprocess.run([sys.executable, str(ROOT / "bench.py"), *args], cwd=ROOT, capture_output=True,
+                          text=True, timeout=timeout)
+
+
+def test_reference_arm_prints_one_contract_line():
+    p = _run("--impl", "reference", "--steps", "1", "--warmup", "1")
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, p.stdout
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference"
+    assert d["unit"] == "ms/FFT" and d["higher_is_better"] is False and d["value"] > 0
+    assert d["steps"] == 1 and d["n_gpus"] == 1 and d["vs_baseline"] is None
+    assert d["config"]["workload"] == "banded_powerlaw_8219" and d["config"]["shape"] == [8219, 8219]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "ms/FFT", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_gpu_arm_fails_loudly_without_a_gpu():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    p = _run("--steps", "1", "--warmup", "0", "--no-cpu-baseline", "--batch-steps", "0", timeout=120)
+    assert p.returncode != 0
+    assert '"value"' not in p.stdout
