@@ -63,3 +63,11 @@ def test_plan_create_without_gpu_fails_loudly():
     coo = gb.COOMatrix(4, 4, [0, 1], [1, 2])
     with pytest.raises(gb.GbspError):
         gb.Plan(coo)
+
+
+def test_missing_library_raises(monkeypatch, tmp_path):
+    # no fallback implementation: without the native library the package refuses to run
+    monkeypatch.setattr(_capi, "_lib", None)
+    monkeypatch.setattr(_capi, "LIB_PATH", tmp_path / "libgbspfft.so")
+    with pytest.raises(RuntimeError, match="native library missing"):
+        _capi.load(build_if_missing=False)
