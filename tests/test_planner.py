@@ -1,0 +1,56 @@
+"""Invariants of the planner's candidate plans, checked on the CPU.
+
+For every shape and length policy, each candidate the planner offers
+(gbsp_plan_candidates) must describe a transform the kernels can run: radices
+the row kernel is compiled for, a channel length (their product) that divides
+the Bluestein length of the policy -- next 3-smooth, 7-smooth or power of two
+>= 2*cols - 1, as the reference computes it (oracle/ref_port.py, pinned to the
+reference's own functions) -- into at most 64 channels, a whole number of
+warps per block and a pass-1 shape index in range.
+"""
+import numpy as np
+import pytest
+
+import cuspfft_gb300 as gb
+from cuspfft_gb300 import tuning
+from oracle import ref_port
+
+SUPPORTED_RADICES = {2, 3, 4, 5, 7, 8, 9, 12, 15, 16, 20, 21, 24, 25, 28, 32, 35, 40}
+MAX_CHANNELS = 64
+
+
+def bluestein_length(cols: int, policy: int) -> int:
+    n = 2 * cols - 1
+    if policy == gb.GBSP_LEN_POW2:
+        return ref_port.next_power_of_two(n)
+    return ref_port.next_smooth(n, seven=policy == gb.GBSP_LEN_7SMOOTH)
+
+
+SHAPES = [(5, 8), (64, 97), (1000, 999), (3001, 2048), (8219, 8219), (16706, 16706), (40421, 40421),
+          (131071, 33), (33, 120001), (5, 200003)]
+
+
+@pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH, gb.GBSP_LEN_POW2])
+@pytest.mark.parametrize("rows,cols", SHAPES)
+def test_candidates_are_runnable(rows, cols, policy):
+    L = bluestein_length(cols, policy)
+    assert gb.next_smooth(2 * cols - 1, policy) == L
+    cands, nr, npp = tuning.candidates(rows, cols, length_policy=policy)
+    assert nr >= 1 and npp >= 1 and len(cands) == nr * npp
+    for c in cands:
+        rad = c.radices()
+        assert rad and set(rad) <= SUPPORTED_RADICES, rad
+        lp = int(np.prod(rad))
+        assert L % lp == 0, (rad, L)
+        assert 1 <= L // lp <= MAX_CHANNELS
+        assert c.rows_threads % 32 == 0 and 32 <= c.rows_threads <= 1024
+        assert 1 <= c.pass1_shape <= gb._capi.GBSP_N_PASS1_SHAPES
+        assert c.length_policy == policy
+
+
+@pytest.mark.parametrize("rows,cols", [(3001, 2048), (8219, 8219)])
+def test_single_channel_when_the_row_fits(rows, cols):
+    # a row that fits one CTA's shared memory runs as one channel
+    for policy in (gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH):
+        cands, _, _ = tuning.candidates(rows, cols, length_policy=policy)
+        assert all(int(np.prod(c.radices())) == bluestein_length(cols, policy) for c in cands)
