@@ -113,3 +113,49 @@ def test_live_reference_host_code():
         assert gb.next_smooth(int(n), 3) == refhost.next_3_smooth(int(n))
         assert gb.next_smooth(int(n), 7) == refhost.next_7_smooth(int(n))
         assert gb.next_smooth(int(n), gb.GBSP_LEN_POW2) == refhost.next_power_of_two(int(n))
+
+
+def test_live_reference_reader_fuzz(tmp_path):
+    """Random Matrix Market files read by this library and by the reference's
+    compiled read_mtx (where the reference tree is present): the same COO,
+    and through make_compact_csc the same CSC, bit for bit.  Header kinds,
+    comment lines, explicit values (zeros included), duplicates and diagonal
+    entries vary; every entry is in range (the reference does not check)."""
+    from oracle import refhost
+    if not refhost.available():
+        pytest.skip("reference host library not built here")
+    g = np.random.default_rng(11)
+    kinds = [("pattern", "general"), ("real", "general"), ("integer", "general"), ("pattern", "symmetric"),
+             ("real", "symmetric"), ("real", "skew-symmetric")]
+    for t in range(60):
+        field, sym = kinds[t % len(kinds)]
+        rows = int(g.integers(1, 200))
+        cols = rows if sym != "general" else int(g.integers(1, 200))
+        n = int(g.integers(0, 600))
+        r = g.integers(1, rows + 1, n)
+        c = g.integers(1, cols + 1, n)
+        if sym != "general":  # lower triangle, as symmetric files store it
+            r, c = np.maximum(r, c), np.minimum(r, c)
+        if n and g.random() < 0.5:  # duplicates
+            k = int(g.integers(1, n + 1))
+            r, c = np.concatenate([r, r[:k]]), np.concatenate([c, c[:k]])
+        lines = [f"%%MatrixMarket matrix coordinate {field} {sym}"]
+        lines += [f"% comment {i}" for i in range(int(g.integers(0, 3)))]
+        lines.append(f"{rows} {cols} {r.size}")
+        for rr, cc in zip(r, c):
+            if field == "pattern":
+                lines.append(f"{rr} {cc}")
+            elif field == "integer":
+                lines.append(f"{rr} {cc} {int(g.integers(-3, 4))}")
+            else:
+                lines.append(f"{rr} {cc} {float(g.choice([0.0, 1.5, -2.25, 1e-300]))}")
+        path = tmp_path / f"f{t}.mtx"
+        path.write_text("\n".join(lines) + "\n")
+        want = refhost.read_mtx(str(path))
+        coo = gb.read_mtx(str(path))
+        assert (coo.rows, coo.cols) == want[:2], path.read_text()[:200]
+        assert np.array_equal(coo.row_idx, want[2]) and np.array_equal(coo.col_idx, want[3]), f"file {t}"
+        sc, cp, ri = refhost.make_compact_csc(coo.rows, coo.cols, want[2], want[3])
+        csc = gb.make_compact_csc(coo)
+        assert np.array_equal(csc.sparse_cols, sc) and np.array_equal(csc.col_ptr, cp)
+        assert np.array_equal(csc.row_idx, ri)
