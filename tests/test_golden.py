@@ -159,3 +159,20 @@ def test_live_reference_reader_fuzz(tmp_path):
         csc = gb.make_compact_csc(coo)
         assert np.array_equal(csc.sparse_cols, sc) and np.array_equal(csc.col_ptr, cp)
         assert np.array_equal(csc.row_idx, ri)
+
+
+def test_live_reference_bluestein_tables_random_lengths():
+    """The oracle's restatement of the reference's chirp and b tables equals
+    the compiled reference functions bit for bit on random lengths (where the
+    reference tree is present), beyond the golden ones."""
+    from oracle import refhost
+    if not refhost.available():
+        pytest.skip("reference host library not built here")
+    g = np.random.default_rng(2)
+    for n in [int(v) for v in g.integers(2, 60000, 30)] + [8219, 16706, 40421, 65535]:
+        for seven in (False, True):
+            L = ref_port.next_smooth(2 * n - 1, seven=seven)
+            assert np.array_equal(ref_port.bluestein_chirp(n).view(np.uint32),
+                                  refhost.bluestein_chirp(n).view(np.uint32)), n
+            assert np.array_equal(ref_port.bluestein_b(n, L).view(np.uint32),
+                                  refhost.bluestein_b(n, L).view(np.uint32)), (n, L)
