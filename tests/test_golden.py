@@ -176,3 +176,18 @@ def test_live_reference_bluestein_tables_random_lengths():
                                   refhost.bluestein_chirp(n).view(np.uint32)), n
             assert np.array_equal(ref_port.bluestein_b(n, L).view(np.uint32),
                                   refhost.bluestein_b(n, L).view(np.uint32)), (n, L)
+
+
+def test_live_reference_factor_and_u16_rule_random():
+    """factor_3_smooth on random 3-smooth lengths and the u16 packing rule on
+    random sizes: the oracle restatement equals the compiled reference."""
+    from oracle import refhost
+    if not refhost.available():
+        pytest.skip("reference host library not built here")
+    g = np.random.default_rng(4)
+    for n in g.integers(1, 200000, 100):
+        m = ref_port.next_smooth(int(n), seven=False)
+        assert refhost.factor_3_smooth(m) == list(ref_port.factor_3_smooth(m)), m
+    for _ in range(100):
+        r, c = int(g.integers(1, 140000)), int(g.integers(1, 140000))
+        assert refhost.can_pack_u16(r, c) == ref_port.can_pack_u16(r, c), (r, c)
