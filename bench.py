@@ -5,9 +5,9 @@
                     [--workload NAME] [--policy 3|7]
 
 One step = one full transform of the workload (pass 1 + Bluestein rows +
-R2C writer) on a synthetic binary matrix with the shape of the reference's
-benzene benchmark (8219 x 8219 symmetric, ~242k nnz, power-law degrees in a
-band).  Prints ONE JSON line (rank 0):
+R2C writer) on a synthetic binary matrix: by default the 16706 x 16706
+symmetric power-law adjacency (~396k nnz, uniform neighbours; 1.1165 GB R2C
+output), the output-bandwidth roofline case.  Prints ONE JSON line (rank 0):
 
   value        device ms per FFT with the CSC and tables resident (plan built
                before the timed region), max over ranks / FFTs of all ranks
@@ -16,8 +16,17 @@ band).  Prints ONE JSON line (rank 0):
                spectrum read back to pinned host memory, plan released
   roofline     the dominant kernel's achieved bytes and FLOPs vs measured peaks
   cpu_baseline the reference's CPU path (dense float32 scatter + 2-D R2C FFT,
-               execute step only) on this host's cores, a bounded sample
+               execute step only) on all of this host's cores and on one
+               core (the reference's FFTW call is single-threaded), bounded
   accuracy     rel-L2 vs the FP64 oracle on sampled output rows
+  reference_gpu the reference's own GPU methods (its kernels compiled for
+               sm_103a, cuFFT for the 7-smooth method) on the same device:
+               tile-loop ms as the reference times it, and rel-L2 of its
+               spectrum vs this library's and vs FP64
+  largest      the 40421 x 40421 adjacency (4-byte indices, 6.5 GB output):
+               device ms per FFT and rel-L2 on sampled rows
+  precision_modes  8219 x 8219: exact-phase + compensated, the default, and
+               plain FP32 sums, each with ms and rel-L2 vs FP64
 
 L2 is flushed (a 512 MiB write) before every timed step, outside the events.
 """
@@ -53,7 +62,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="banded_powerlaw_8219", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="uniform_powerlaw_16706", choices=sorted(WORKLOADS))
     ap.add_argument("--policy", type=int, default=7, choices=[3, 7])
     ap.add_argument("--u-tile", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -62,6 +71,10 @@ def parse():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=5,
                     help="timed passes of the 64-matrix batched workload (0 skips it)")
+    ap.add_argument("--largest-steps", type=int, default=5,
+                    help="timed transforms of the 40421^2 workload (0 skips it)")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference's GPU methods")
+    ap.add_argument("--no-precision-modes", action="store_true")
     return ap.parse_args()
 
 
@@ -137,9 +150,38 @@ def measured_peaks() -> dict:
 def cpu_baseline(coo, budget: float) -> dict:
     from oracle import ref_port
     t = ref_port.time_cpu_baseline(coo.rows, coo.cols, coo.row_idx, coo.col_idx, budget_s=budget)
+    t1 = ref_port.time_cpu_baseline(coo.rows, coo.cols, coo.row_idx, coo.col_idx, budget_s=budget, workers=1,
+                                    max_reps=5)
     return {"value": round(t["ms_median"], 3), "unit": "ms/FFT", "cores": t["workers"], "kind": "port",
             "sample": f"{t['reps']} full transforms of the workload; scipy.fft.rfft2 float32 (pocketfft) "
-                      f"standing in for FFTW fftwf_execute, workers={t['workers']}, execute step timed"}
+                      f"standing in for FFTW fftwf_execute, workers={t['workers']}, execute step timed",
+            "single_thread": {"value": round(t1["ms_median"], 3), "unit": "ms/FFT", "cores": 1,
+                              "sample": f"{t1['reps']} full transforms, workers=1 (the reference's FFTW call is "
+                                        "single-threaded, src/cpu_reference.cpp:36-45)"}}
+
+
+def reference_gpu(coo, policy_out, us, exact, n_times: int = 3) -> dict:
+    """The reference's own GPU methods on this device (oracle/refgpu.py): its
+    kernels compiled for sm_103a and launched in its host code's order; the
+    7-smooth method calls cuFFT as the reference does.  Tile-loop ms (CUDA
+    events, device synchronised, as the reference times it), at the
+    reference header's u_tile 128 and its CLI default 1024."""
+    from oracle import fp64, refgpu
+    if not refgpu.available():
+        return {"unavailable": "reference kernels not built (oracle/_ref)"}
+    res = {}
+    for method, name in ((3, "sparse_fft_csc_bluestein_mixed_radix"), (7, "sparse_fft_csc_bluestein_cufft_smooth")):
+        ent = {"fft_len": refgpu.fft_len(coo.cols, method)}
+        for ut in (128, 1024):
+            spec, times = refgpu.run(coo.rows, coo.cols, coo.row_idx, coo.col_idx, method, u_tile=ut,
+                                     n_times=n_times)
+            ent[f"ms_u_tile_{ut}"] = round(statistics.median(times), 3)
+        ent["rel_l2_vs_fp64"] = fp64.rel_l2(spec[us], exact)
+        if method in policy_out:
+            ent["rel_l2_vs_this_library"] = fp64.rel_l2(policy_out[method], spec)
+        res[name] = ent
+        del spec
+    return res
 
 
 def run_reference(args, world, rank):
@@ -196,6 +238,60 @@ def small_matrices(synthetic, count: int = 256, lo: int = 100, hi: int = 1000, s
         d = float(math.exp(g.uniform(math.log(1e-3), math.log(3e-2))))
         mats.append(synthetic.uniform_matrix(r, c, max(1, int(r * c * d)), 1000 + i))
     return mats
+
+
+def sample_rows(np, rows: int, n: int = 28):
+    g = np.random.default_rng(0)
+    return np.unique(np.concatenate([[0, 1, rows // 2, rows - 1], g.integers(0, rows, n)]))
+
+
+def run_single(args, torch, gb, synthetic, name, policy, steps, flush, **opts) -> dict:
+    """Device ms per FFT of one workload (plan resident, L2 flushed before
+    each step) and its rel-L2 vs FP64 on sampled rows."""
+    import numpy as np
+    from oracle import fp64
+    coo = synthetic.config_matrix(name)
+    with gb.Plan(coo, length_policy=policy, **opts) as plan:
+        info = plan.info
+        out = plan.empty_output()
+        for _ in range(max(args.warmup, 3)):
+            plan.execute(out)
+        stream = torch.cuda.current_stream()
+        ms = []
+        for s in range(steps):
+            flush.fill_(s & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.execute(out)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        p1, rows = plan.execute_profiled(out)
+        flags = plan.error_flags()
+        us = sample_rows(np, coo.rows, 12)
+        got = out[torch.as_tensor(us, device="cuda")].cpu().numpy()[:, : coo.cols // 2 + 1]
+        del out
+    ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, us)
+    return {"workload": name, "description": WORKLOADS[name], "ms_per_fft": round(statistics.median(ms), 4),
+            "steps": steps, "phase_ms": {"k_twiddle_sum": round(p1, 4), "k_bluestein_rows": round(rows, 4)},
+            "fft_len": info["fft_len"], "channels": info["channels"], "radix": info["radix"],
+            "index_bytes": info["index_bytes"], "output_bytes": coo.rows * info["output_pitch"] * 8,
+            "rel_l2_vs_fp64": fp64.rel_l2(got, ref), "rows_sampled": int(us.size), "error_flags": flags}
+
+
+def precision_modes(args, torch, gb, synthetic, flush) -> dict:
+    """The 8219^2 benchmark matrix in three pass-1 arithmetic forms, each with
+    its device ms per FFT and rel-L2 vs FP64: exact integer phases with every
+    twiddle a table lookup plus Kahan sums for high-degree columns; the
+    default (table lookup every 4th row, recurrence between, Kahan); plain
+    FP32 sums (recurrence, no compensation)."""
+    res = {}
+    for key, opts in (("exact_phase_compensated", {"exact_phases": 1}), ("default", {}),
+                      ("plain_fp32", {"kahan_min_degree": -1})):
+        r = run_single(args, torch, gb, synthetic, "banded_powerlaw_8219", 7, 5, flush, **opts)
+        res[key] = {"ms_per_fft": r["ms_per_fft"], "k_twiddle_sum_ms": r["phase_ms"]["k_twiddle_sum"],
+                    "rel_l2_vs_fp64": r["rel_l2_vs_fp64"]}
+    return res
 
 
 def batch_vs_plain(args, torch, gb, mats) -> tuple[float, float, object]:
@@ -395,12 +491,34 @@ def main():
     acc = None
     if not args.no_accuracy and rank == 0:
         from oracle import fp64
-        g = np.random.default_rng(0)
-        us = np.unique(np.concatenate([[0, 1, coo.rows // 2, coo.rows - 1], g.integers(0, coo.rows, 28)]))
+        us = sample_rows(np, coo.rows)
         ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, us)
         got = out[torch.as_tensor(us, device="cuda")].cpu().numpy()[:, : coo.cols // 2 + 1]
         st = fp64.check_stats(got, ref)
         acc = {"rel_l2_vs_fp64": st["rel_l2"], "max_abs": st["max_abs"], "rows_sampled": int(us.size)}
+
+    ref_gpu = None
+    if rank == 0 and not args.no_ref_gpu and not args.no_accuracy:
+        outs = {args.policy: out[:, : coo.cols // 2 + 1].cpu().numpy()}
+        other = 3 if args.policy == 7 else 7
+        with gb.Plan(coo, length_policy=other, csc=csc) as oplan:
+            o2 = oplan.empty_output()
+            oplan.execute(o2)
+            torch.cuda.synchronize()
+            outs[other] = o2[:, : coo.cols // 2 + 1].cpu().numpy()
+            del o2
+        ref_gpu = reference_gpu(coo, outs, us, ref)
+        ref_gpu["this_library_rel_l2_vs_fp64"] = {m: fp64.rel_l2(o[us], ref) for m, o in outs.items()}
+        del outs
+
+    largest = None
+    if rank == 0 and args.largest_steps > 0 and args.workload != "uniform_powerlaw_40421":
+        largest = run_single(args, torch, gb, synthetic, "uniform_powerlaw_40421", args.policy, args.largest_steps,
+                             flush, index_bytes=4)
+
+    modes = None
+    if rank == 0 and not args.no_precision_modes:
+        modes = precision_modes(args, torch, gb, synthetic, flush)
 
     batched = None
     if rank == 0 and args.batch_steps > 0:
@@ -426,7 +544,7 @@ def main():
             "output_gbs": round(out_bytes / (ms_per_step * 1e-3) / 1e9, 1),
             "gpu_launches": 2 * n_tiles * args.steps,
             "clocks": clk, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "accuracy": acc,
-            "batched": batched,
+            "reference_gpu": ref_gpu, "largest": largest, "precision_modes": modes, "batched": batched,
         }
         print(json.dumps(line), flush=True)
     plan.close()

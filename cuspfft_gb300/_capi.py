@@ -35,7 +35,7 @@ EXPORTED = (
     "gbsp_version", "gbsp_status_string", "gbsp_last_error", "gbsp_read_mtx", "gbsp_free",
     "gbsp_build_compact_csc", "gbsp_next_smooth", "gbsp_plan_create", "gbsp_plan_get_info",
     "gbsp_plan_destroy", "gbsp_execute", "gbsp_execute_profiled", "gbsp_column_sums",
-    "gbsp_plan_error_flags", "gbsp_execute_noalloc", "gbsp_batch_create", "gbsp_batch_set_outputs",
+    "gbsp_plan_error_flags", "gbsp_device_flags_status", "gbsp_execute_noalloc", "gbsp_batch_create", "gbsp_batch_set_outputs",
     "gbsp_batch_execute", "gbsp_batch_graph_launch", "gbsp_batch_plan_info", "gbsp_batch_error_flags",
     "gbsp_batch_destroy", "gbsp_plan_candidates", "gbsp_plan_features", "gbsp_autotune", "gbsp_mlp_param_count",
     "gbsp_mlp_forward", "gbsp_mlp_work_floats", "gbsp_mlp_backward", "gbsp_mlp_adam", "gbsp_cost_model_set",
@@ -57,6 +57,7 @@ class GbspOptions(C.Structure):
         ("planner", C.c_int),
         ("channel_mode", C.c_int),
         ("stream_tile_rows", C.c_int),
+        ("exact_phases", C.c_int),
     ]
 
     def radices(self) -> tuple:
@@ -71,6 +72,7 @@ class GbspPlanInfo(C.Structure):
         ("output_pitch", C.c_int), ("half_rows", C.c_int), ("u_tile", C.c_int),
         ("index_bytes", C.c_int), ("row_table_mode", C.c_int), ("rows_threads", C.c_int),
         ("device_bytes", C.c_size_t), ("pass1_shape", C.c_int), ("planner", C.c_int), ("channel_mode", C.c_int),
+        ("exact_phases", C.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -131,6 +133,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                            C.POINTER(C.c_float)]
     lib.gbsp_column_sums.argtypes = [vp, i32, i32, vp, C.c_size_t, vp]
     lib.gbsp_plan_error_flags.argtypes = [vp, ip]
+    lib.gbsp_device_flags_status.argtypes = [i32]
     lib.gbsp_execute_noalloc.argtypes = [vp, vp, C.c_size_t, vp]
     lib.gbsp_batch_create.argtypes = [i32, C.POINTER(GbspMatrix), C.POINTER(GbspOptions), vp, C.POINTER(vp)]
     lib.gbsp_batch_set_outputs.argtypes = [vp, C.POINTER(vp), C.POINTER(C.c_size_t)]

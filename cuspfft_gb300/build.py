@@ -27,8 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               f"-I{INCLUDE}", f"-I{CSRC}"]
 
-LIB_SOURCES = ["gbsp_rows_multi.cu", "gbsp_rows_seq.cu", "gbsp_rows.cu", "gbsp_pass1.cu", "gbsp_plan.cu", "gbsp_planner.cu", "gbsp_mlp.cu",
-               "gbsp_host.cpp", "sparse_fft_api.cu"]
+LIB_SOURCES = ["gbsp_rows_multi.cu", "gbsp_rows_seq.cu", "gbsp_rows.cu", "gbsp_pass1.cu", "gbsp_pass1_exact.cu",
+               "gbsp_plan.cu", "gbsp_planner.cu", "gbsp_mlp.cu", "gbsp_host.cpp", "sparse_fft_api.cu"]
 CLI_SOURCES = ["cli_main.cpp"]
 
 

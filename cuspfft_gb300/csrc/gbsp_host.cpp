@@ -71,6 +71,16 @@ int gbsp_last_error(char* buf, size_t buflen) {
     return GBSP_OK;
 }
 
+int gbsp_device_flags_status(int flags) {
+    if (flags == 0) return GBSP_OK;
+    std::string why;
+    if (flags & 1) why += "a bounded device wait gave up";
+    if (flags & 2) why += std::string(why.empty() ? "" : "; ") + "a stage radix the row kernel was not compiled for";
+    if (flags & ~3) why += std::string(why.empty() ? "" : "; ") + "unknown bits";
+    return set_error(GBSP_ERR_CUDA, "device error flags " + std::to_string(flags) + " (" + why +
+                                        "): the transform's result is not valid");
+}
+
 int gbsp_next_smooth(int n, int policy) {
     if (policy != GBSP_LEN_3SMOOTH && policy != GBSP_LEN_7SMOOTH && policy != GBSP_LEN_POW2) return -1;
     long m = gbsp::next_smooth(n, policy);

@@ -145,7 +145,10 @@ struct NzInfo {
     float wx, wy;
 };
 
-template <typename IDX, int TAB, bool BIG, int KU>
+// EXACT: every twiddle is the table entry at its exact phase
+// (u*r) mod rows -- the phase of row u + 32*(kk+1) is that of row u + 32*kk
+// plus (32*r) mod rows, reduced by one compare -- with no recurrence.
+template <typename IDX, int TAB, bool BIG, int KU, bool EXACT>
 __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx, int beg, int end,
                                                  const float2* tab, NzInfo* info, uint32_t u_lane,
                                                  uint32_t rows, uint32_t magic, unsigned long long magic64,
@@ -161,10 +164,45 @@ __device__ __forceinline__ void column_sums_warp(const IDX* __restrict__ row_idx
             const uint32_t r = (uint32_t)row_idx[p0 + lane];
             const uint32_t d = mulmod_rows<BIG>(32u, r, rows, magic, magic64);
             const float2 wd = row_twiddle<TAB>(tab, d, rows, hr);
-            const uint32_t st = (KU > P1_RESEED) ? mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic, magic64) : 0u;
+            const uint32_t st = EXACT ? d
+                                : (KU > P1_RESEED) ? mulmod_rows<BIG>((uint32_t)P1_RESEED, d, rows, magic, magic64) : 0u;
             info[lane] = NzInfo{r, st, -wd.x, -wd.y};  // the step, negated
         }
         __syncwarp();
+        if constexpr (EXACT) {
+            float2 blk[KU];
+#pragma unroll
+            for (int i = 0; i < KU; i++) blk[i] = make_float2(0.f, 0.f);
+#pragma unroll 2
+            for (int i = 0; i < cnt; i++) {
+                const NzInfo z = info[i];
+                uint32_t p = mulmod_rows<BIG>(u_lane, z.r, rows, magic, magic64);
+#pragma unroll
+                for (int kk = 0; kk < KU; kk++) {
+                    blk[kk] = __fadd2_rn(blk[kk], row_twiddle<TAB>(tab, p, rows, hr));
+                    const uint32_t pn = p + z.step;
+                    p = min(pn, pn - rows);
+                }
+            }
+            __syncwarp();
+            if (compensated) {
+#pragma unroll
+                for (int kk = 0; kk < KU; kk++) {
+                    float y = blk[kk].x - cmp[kk].x;
+                    float t = acc[kk].x + y;
+                    cmp[kk].x = (t - acc[kk].x) - y;
+                    acc[kk].x = t;
+                    y = blk[kk].y - cmp[kk].y;
+                    t = acc[kk].y + y;
+                    cmp[kk].y = (t - acc[kk].y) - y;
+                    acc[kk].y = t;
+                }
+            } else {
+#pragma unroll
+                for (int kk = 0; kk < KU; kk++) { acc[kk].x += blk[kk].x; acc[kk].y += blk[kk].y; }
+            }
+            continue;
+        }
         // Rows kk = 4g+1 and 4g+2 are carried negated, so every operation
         // below is a plain packed FP32x2 add or FMA with no operand negation:
         //   n1 = w0 * (-z)          = -w1
@@ -259,7 +297,7 @@ __device__ __forceinline__ long p1_items(const P1Args& a, int ublk) {
 // Work item `it` of one matrix: all tasks of one (row block, column window),
 // then the window's tile written to S.  Whole CTA; tab holds the matrix's
 // twiddle table.
-template <typename IDX, int TAB, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU, bool EXACT>
 __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage, NzInfo* info_all,
                                         const float2* tab, P1Shared& sh) {
     constexpr int UBLK = 32 * KU;
@@ -288,7 +326,7 @@ __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage,
         const int2 range = a.win_task[(size_t)w * vmax + i];
         const int col = a.win_task_col[(size_t)w * vmax + i];
         float2 acc[KU];
-        column_sums_warp<IDX, TAB, BIG, KU>(row_idx, range.x, range.y, tab, info, u_lane,
+        column_sums_warp<IDX, TAB, BIG, KU, EXACT>(row_idx, range.x, range.y, tab, info, u_lane,
                                                  (uint32_t)a.rows, a.magic, a.magic64, lane,
                                                  a.kahan_min > 0 && range.y - range.x >= a.kahan_min, acc);
 #pragma unroll
@@ -325,7 +363,7 @@ __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage,
     __syncthreads();
 }
 
-template <typename IDX, int TAB, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU, bool EXACT>
 __global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
     extern __shared__ float4 smem_raw[];
     __shared__ P1Shared sh;
@@ -344,7 +382,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
         __syncthreads();
         const long it = sh.item;
         if (it >= nitems) break;
-        p1_item<IDX, TAB, BIG, KU>(a, it, stage, info_all, tab, sh);
+        p1_item<IDX, TAB, BIG, KU, EXACT>(a, it, stage, info_all, tab, sh);
     }
     // the last CTA out (every other one has stopped taking items) rearms the
     // queue for the next launch
@@ -362,7 +400,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1) k_twiddle_sum(P1Args a) {
 // one item per grab.  Items are grabbed in increasing order, so a CTA moves
 // forward through the matrices and reloads the twiddle table only when it
 // enters a new one.  *queue must be 0 at launch.
-template <typename IDX, int TAB, bool BIG, int KU>
+template <typename IDX, int TAB, bool BIG, int KU, bool EXACT>
 __global__ void __launch_bounds__(P1_THREADS, 1)
 k_twiddle_sum_batch(const P1Args* __restrict__ args, const long* __restrict__ item_begin, int nmat,
                     unsigned long long* queue) {
@@ -399,7 +437,7 @@ k_twiddle_sum_batch(const P1Args* __restrict__ args, const long* __restrict__ it
         }
         NzInfo* info_all = reinterpret_cast<NzInfo*>(stage + (size_t)32 * KU * p1_pitch(cur.cw));
         float2* tab = reinterpret_cast<float2*>(info_all + P1_WARPS * 32);
-        p1_item<IDX, TAB, BIG, KU>(cur, it - item_begin[m], stage, info_all, tab, sh);
+        p1_item<IDX, TAB, BIG, KU, EXACT>(cur, it - item_begin[m], stage, info_all, tab, sh);
     }
 }
 

@@ -38,12 +38,13 @@ int device_limits(int dev, DeviceLimits* out);
 // earlier one.  Done once per (kernel, device).
 int allow_full_smem(const void* kern);
 
-// ---- pass 1 (gbsp_pass1.cu): one compiled kernel per
-// (index bytes, table layout, 64-bit phases, rows per lane)
+// ---- pass 1 (gbsp_pass1.cu, gbsp_pass1_exact.cu): one compiled kernel per
+// (index bytes, table layout, 64-bit phases, rows per lane, phase mode)
 struct P1Kernel {
     int idx_bytes, tab;
     bool big;
     int ku;
+    bool exact;  // every twiddle an exact table lookup (no recurrence)
 };
 // CTAs of k_twiddle_sum resident per SM with `smem` bytes (raises the limit)
 int p1_blocks_per_sm(const P1Kernel& k, size_t smem, int* nb);

@@ -37,6 +37,7 @@ struct gbsp_plan_s {
     gbsp::FFTDesc fd{};
     int half_rows = 0, u_tile = 0, out_cols = 0, out_pitch = 0;
     int idx_bytes = 2, tab_mode = 0, big = 0, kahan_min = 64, ntab = 0;  // tab_mode: gbsp::TAB_*
+    int exact = 0;                   // pass-1 twiddles all exact table lookups (no recurrence)
     int p1_ku = 8, p1_cw = 32;       // pass-1 rows per lane (x32 per item) and window width
     int p1_shape = 1;                // 1-based index of (p1_ku, p1_cw, tab_mode) in the shape table
     int planner = GBSP_PLANNER_MODEL;
@@ -167,7 +168,7 @@ void free_plan(gbsp_plan_s* p) {
 inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 gbsp::P1Kernel p1_kernel(const gbsp_plan_s* p) {
-    return gbsp::P1Kernel{p->idx_bytes, p->tab_mode, p->big != 0, p->p1_ku};
+    return gbsp::P1Kernel{p->idx_bytes, p->tab_mode, p->big != 0, p->p1_ku, p->exact != 0};
 }
 
 // sizes pass 1's persistent grid (and raises the kernel's shared-memory limit)
@@ -354,6 +355,8 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->out_cols = p->cols / 2 + 1;
     p->out_pitch = (p->out_cols + 3) / 4 * 4;
     p->u_tile = (o.u_tile > 0) ? std::min(o.u_tile, p->half_rows) : p->half_rows;
+    if (o.exact_phases < 0 || o.exact_phases > 1) return set_error(GBSP_ERR_INVALID, "exact_phases must be 0 or 1");
+    p->exact = o.exact_phases;
     p->kahan_min = (o.kahan_min_degree != 0) ? o.kahan_min_degree : 64;
     if (p->kahan_min < 0) p->kahan_min = 0;  // 0 disables compensation in the kernel
     int ib = o.index_bytes ? o.index_bytes : ((p->rows <= 65536 && p->cols <= 65536) ? 2 : 4);
@@ -583,6 +586,15 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     return GBSP_OK;
 }
 
+// Reads and clears the plan's device error word (synchronous) and turns it
+// into a status (gbsp_device_flags_status)
+int read_device_flags(const gbsp_plan_s* p) {
+    int flags = 0;
+    GB_CUDA(cudaMemcpy(&flags, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flags) GB_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+    return gbsp_device_flags_status(flags);
+}
+
 int check_out(const gbsp_plan_s* p, const void* d_out, size_t out_pitch, const char* who) {
     if (!p || !d_out) return set_error(GBSP_ERR_INVALID, std::string(who) + ": null argument");
     if (out_pitch < (size_t)p->out_cols || (out_pitch & 1))
@@ -653,6 +665,7 @@ int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
     info->pass1_shape = p->p1_shape;
     info->planner = p->planner;
     info->channel_mode = p->K == 1 ? 0 : (p->row_mode == gbsp::ROW_CLUSTER ? 1 : 2);
+    info->exact_phases = p->exact;
     return GBSP_OK;
 }
 
@@ -714,9 +727,7 @@ int gbsp_execute_profiled(gbsp_plan_t p, void* d_out, size_t out_pitch, void* st
     for (auto e : ev)
         if (e) cudaEventDestroy(e);
     if (rc != GBSP_OK) return set_error(rc, "gbsp_execute_profiled: CUDA failure");
-    int flags = 0;
-    GB_CUDA(cudaMemcpy(&flags, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (flags) return set_error(GBSP_ERR_CUDA, "gbsp_execute_profiled: a bounded device wait timed out");
+    if ((rc = read_device_flags(p))) return rc;
     *ms_pass1 = a;
     *ms_rows = b;
     return GBSP_OK;
@@ -796,8 +807,12 @@ extern "C" int gbsp_execute_noalloc(gbsp_plan_t p, void* d_out, size_t out_pitch
     void* scratch = nullptr;
     if ((rc = noalloc_scratch_address(dev, &scratch))) return rc;
     // Tiles sized to the array.  Nothing in it has to start at zero: pass 1
-    // writes every element of a tile row that the row kernel reads.
-    const int tile = (int)std::min<size_t>((size_t)p->u_tile, NOALLOC_SCRATCH_BYTES / row_bytes);
+    // writes every element of a tile row that the row kernel reads.  Pass 1
+    // computes whole blocks of 32*KU rows, so a tile whose last block would
+    // be less than half used is cut back to a whole number of blocks.
+    int tile = (int)std::min<size_t>((size_t)p->u_tile, NOALLOC_SCRATCH_BYTES / row_bytes);
+    const int ublk = 32 * p->p1_ku;
+    if (tile < p->u_tile && tile >= ublk && tile % ublk < ublk / 2) tile -= tile % ublk;
     cudaStream_t st = (cudaStream_t)stream;
     for (int u0 = 0; u0 < p->half_rows; u0 += tile) {
         const int n = std::min(tile, p->half_rows - u0);
@@ -825,7 +840,7 @@ struct gbsp_batch_s {
     std::vector<gbsp_plan_s*> plans;
     std::vector<int> order;      // queue order (batched matrices, costliest rows first)
     std::vector<int> separate;   // matrices that run through their own plan
-    int p1_shape = 1, ku = 8, cw = 32, tab = 0, idx_bytes = 2, big = 0;
+    int p1_shape = 1, ku = 8, cw = 32, tab = 0, idx_bytes = 2, big = 0, exact = 0;
     int p1_grid = 0;
     size_t p1_smem = 0;
     // Row launches: one per class of matrices that share a block size and a
@@ -872,7 +887,7 @@ int batch_alloc(gbsp_batch_s* b, void** ptr, size_t bytes) {
 
 // prepare: size the batched pass-1 grid; else launch it
 int p1b_dispatch(gbsp_batch_s* b, bool prepare, int sms, cudaStream_t st) {
-    const gbsp::P1Kernel k{b->idx_bytes, b->tab, b->big != 0, b->ku};
+    const gbsp::P1Kernel k{b->idx_bytes, b->tab, b->big != 0, b->ku, b->exact != 0};
     if (prepare) {
         int nb = 0;
         if (int rc = gbsp::p1_batch_blocks_per_sm(k, b->p1_smem, &nb)) return rc;
@@ -939,6 +954,7 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
     }
     b->idx_bytes = u32 ? 4 : 2;
     b->big = max_rows > 65535;
+    b->exact = (opts && opts->exact_phases == 1) ? 1 : 0;
     {
         const int tmode = opts ? opts->row_table_mode : 0;
         std::vector<int> fit = gbsp::fitting_p1_shapes(max_rows, smem_cap, tmode);
@@ -1174,7 +1190,10 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
     }
     if (p->stream_slab_bytes < slab_bytes) {
         for (int b = 0; b < 2; b++) {
-            if (p->stream_slab[b] && p->stream_slab_owned) cudaFree(p->stream_slab[b]);
+            if (p->stream_slab[b] && p->stream_slab_owned) {
+                cudaFree(p->stream_slab[b]);
+                p->device_bytes -= p->stream_slab_bytes;
+            }
             p->stream_slab[b] = nullptr;
         }
         p->stream_slab_bytes = 0;
@@ -1186,6 +1205,7 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
                 p->stream_slab[b] = nullptr;
                 return set_error(GBSP_ERR_ALLOC, std::string("gbsp_execute_to_host: slab: ") + cudaGetErrorString(e));
             }
+            p->device_bytes += slab_bytes;
         }
         p->stream_slab_bytes = slab_bytes;
     }
@@ -1232,5 +1252,5 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
     if (e1 != cudaSuccess || e2 != cudaSuccess)
         return set_error(GBSP_ERR_CUDA, std::string("gbsp_execute_to_host: ") +
                                             cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
-    return GBSP_OK;
+    return read_device_flags(p);
 }

@@ -67,20 +67,26 @@ struct GraphHolder {
     }
 };
 
-// cudaMemGetInfo delta between construction and finish() -- the reference's
-// memory metric (src/sparse_fft_bluestein.cu:7-20).
-struct MemDelta {
-    size_t base_free = 0;
-    MemDelta() {
-        size_t total = 0;
-        if (cudaMemGetInfo(&base_free, &total) != cudaSuccess) base_free = 0;
-    }
-    size_t finish() const {
-        size_t now = 0, total = 0;
-        if (base_free == 0 || cudaMemGetInfo(&now, &total) != cudaSuccess) return 0;
-        return now < base_free ? base_free - now : 0;
-    }
-};
+// The reference's memory metric (DeviceMemPeak, src/sparse_fft_bluestein.cu:7-20)
+// is the cudaMemGetInfo delta at the end of the call: every buffer the call
+// still holds then (tables, scratch, output).  Here those are the plan's
+// device memory and the output, counted directly: a cudaMemGetInfo delta
+// cannot see plan memory that the library's pool hands out again, so from
+// the second call on it would report little more than the output.
+size_t working_set(gbsp_plan_t p, size_t out_bytes) {
+    gbsp_plan_info info;
+    check(gbsp_plan_get_info(p, &info), "gbsp_plan_get_info");
+    return info.device_bytes + out_bytes;
+}
+
+// Reads and clears the plan's device error word once the call's work is
+// done (outside the timed region) and throws if a kernel reported one, as
+// the reference throws on a CUDA failure (include/sparse_fft_internal.cuh:16-22).
+void check_device_flags(gbsp_plan_t p, const char* who) {
+    int flags = 0;
+    check(gbsp_plan_error_flags(p, &flags), "gbsp_plan_error_flags");
+    check(gbsp_device_flags_status(flags), who);
+}
 
 void make_plan(const COOMatrix& coo, int u_tile, int policy, PlanHolder& ph, gbsp_plan_info& info) {
     if (u_tile <= 0) throw std::runtime_error("CSC tile size must be positive");
@@ -95,7 +101,6 @@ void make_plan(const COOMatrix& coo, int u_tile, int policy, PlanHolder& ph, gbs
 }
 
 SparseFFTResult run_method(const COOMatrix& coo, int u_tile, int policy) {
-    MemDelta mem;
     PlanHolder ph;
     gbsp_plan_info info;
     make_plan(coo, u_tile, policy, ph, info);
@@ -110,8 +115,9 @@ SparseFFTResult run_method(const COOMatrix& coo, int u_tile, int policy) {
     cuda_check(cudaEventSynchronize(ev.b), "cudaEventSynchronize");
     float ms = 0.f;
     cuda_check(cudaEventElapsedTime(&ms, ev.a, ev.b), "cudaEventElapsedTime");
+    check_device_flags(ph.p, "gbsp_execute");
     SparseFFTResult r;
-    r.mem_bytes = mem.finish();
+    r.mem_bytes = working_set(ph.p, (size_t)coo.rows * info.output_pitch * sizeof(cuFloatComplex));
     r.output_cols = info.output_pitch;
     r.ms = ms;
     r.d_output = (cuFloatComplex*)out.release();
@@ -119,7 +125,6 @@ SparseFFTResult run_method(const COOMatrix& coo, int u_tile, int policy) {
 }
 
 SparseFFTResult run_graph(const COOMatrix& coo, int u_tile, int policy) {
-    MemDelta mem;
     PlanHolder ph;
     gbsp_plan_info info;
     make_plan(coo, u_tile, policy, ph, info);
@@ -143,8 +148,9 @@ SparseFFTResult run_graph(const COOMatrix& coo, int u_tile, int policy) {
     cuda_check(cudaEventSynchronize(ev.b), "cudaEventSynchronize");
     float ms = 0.f;
     cuda_check(cudaEventElapsedTime(&ms, ev.a, ev.b), "cudaEventElapsedTime");
+    check_device_flags(ph.p, "graph replay");
     SparseFFTResult r;
-    r.mem_bytes = mem.finish();
+    r.mem_bytes = working_set(ph.p, (size_t)coo.rows * info.output_pitch * sizeof(cuFloatComplex));
     r.output_cols = info.output_pitch;
     r.ms = ms;
     r.d_output = (cuFloatComplex*)out.release();
@@ -162,7 +168,6 @@ struct PinnedBuf {
 // is returned in h_output with d_output = nullptr, as the reference's
 // streaming methods do (src/sparse_fft_bluestein.cu:1276-1296).
 SparseFFTResult run_streaming(const COOMatrix& coo, int u_tile, int policy) {
-    MemDelta mem;
     PlanHolder ph;
     gbsp_plan_info info;
     make_plan(coo, u_tile, policy, ph, info);
@@ -178,7 +183,7 @@ SparseFFTResult run_streaming(const COOMatrix& coo, int u_tile, int policy) {
     float ms = 0.f;
     cuda_check(cudaEventElapsedTime(&ms, ev.a, ev.b), "cudaEventElapsedTime");
     SparseFFTResult r;
-    r.mem_bytes = mem.finish();
+    r.mem_bytes = working_set(ph.p, 0);  // the spectrum is in host memory
     r.output_cols = info.output_pitch;
     r.ms = ms;
     r.d_output = nullptr;

@@ -150,7 +150,7 @@ class Plan:
     def __init__(self, coo: COOMatrix, *, length_policy: int = 0, u_tile: int = 0,
                  kahan_min_degree: int = 0, index_bytes: int = 0, max_channel_len: int = 0,
                  rows_threads: int = 0, row_table_mode: int = 0, radix=None, pass1_shape: int = 0,
-                 channel_mode: int = 0, stream_tile_rows: int = 0, planner=None,
+                 channel_mode: int = 0, stream_tile_rows: int = 0, exact_phases: int = 0, planner=None,
                  options: Optional[GbspOptions] = None, stream=None,
                  csc: Optional[CompactCSC] = None):
         lib = load()
@@ -162,7 +162,7 @@ class Plan:
                          kahan_min_degree=kahan_min_degree, index_bytes=index_bytes,
                          max_channel_len=max_channel_len, rows_threads=rows_threads,
                          row_table_mode=row_table_mode, pass1_shape=pass1_shape, channel_mode=channel_mode,
-                         stream_tile_rows=stream_tile_rows)
+                         stream_tile_rows=stream_tile_rows, exact_phases=exact_phases)
         cp = np.ascontiguousarray(csc.col_ptr, np.int32)
         ri = np.ascontiguousarray(csc.row_idx if coo.nnz else np.zeros(1, np.int32), np.int32)
         sc = np.ascontiguousarray(csc.sparse_cols if csc.n_sparse_cols else np.zeros(1, np.int32),
@@ -215,6 +215,18 @@ class Plan:
         check(self._lib.gbsp_plan_error_flags(self._h, C.byref(f)), "gbsp_plan_error_flags")
         return f.value
 
+    def check_device_flags(self, who: str = "transform") -> None:
+        """Reads and clears the device error word; raises GbspError if a
+        kernel of this plan reported an error since the last read."""
+        check(self._lib.gbsp_device_flags_status(self.error_flags()), who)
+
+    @property
+    def device_bytes(self) -> int:
+        """Device memory the plan holds now (its allocation and any streaming slabs)."""
+        info = GbspPlanInfo()
+        check(self._lib.gbsp_plan_get_info(self._h, C.byref(info)), "gbsp_plan_get_info")
+        return int(info.device_bytes)
+
     def column_sums(self, u0: int, n_rows: int, out, stream=None) -> None:
         """S[u-u0][c] for u in [u0, u0+n_rows) and every column c (pitch >= cols rounded up to even)."""
         check(self._lib.gbsp_column_sums(self._h, u0, n_rows, C.c_void_p(out.data_ptr()), out.shape[1],
@@ -248,7 +260,7 @@ class Batch:
 
     def __init__(self, coos, *, length_policy: int = 0, kahan_min_degree: int = 0,
                  index_bytes: int = 0, max_channel_len: int = 0, row_table_mode: int = 0, pass1_shape: int = 0,
-                 planner=None, stream=None):
+                 exact_phases: int = 0, planner=None, stream=None):
         lib = load()
         self._lib = lib
         self._h = C.c_void_p()
@@ -267,7 +279,7 @@ class Batch:
             mats[i] = GbspMatrix(coo.rows, coo.cols, csc.n_sparse_cols, coo.nnz, _ip(cp), _ip(ri), _ip(sc))
         o = make_options(None, planner=planner, length_policy=length_policy, kahan_min_degree=kahan_min_degree,
                          index_bytes=index_bytes, max_channel_len=max_channel_len, row_table_mode=row_table_mode,
-                         pass1_shape=pass1_shape)
+                         pass1_shape=pass1_shape, exact_phases=exact_phases)
         check(lib.gbsp_batch_create(n, mats, C.byref(o), _stream_handle(stream), C.byref(self._h)),
               "gbsp_batch_create")
         self.infos = []
@@ -333,7 +345,6 @@ def _run_method(coo: COOMatrix, u_tile: int, policy: int) -> SparseFFTResult:
     import torch
     if u_tile <= 0:
         raise RuntimeError("CSC tile size must be positive")
-    free0, _ = torch.cuda.mem_get_info()
     with Plan(coo, length_policy=policy, u_tile=u_tile) as plan:
         out = plan.empty_output()
         torch.cuda.synchronize()
@@ -342,8 +353,11 @@ def _run_method(coo: COOMatrix, u_tile: int, policy: int) -> SparseFFTResult:
         plan.execute(out)
         e1.record()
         e1.synchronize()
-        free1, _ = torch.cuda.mem_get_info()
-        return SparseFFTResult(out, plan.output_pitch, e0.elapsed_time(e1), max(0, free0 - free1))
+        plan.check_device_flags("gbsp_execute")
+        # the reference's metric is the device memory the call holds at its
+        # end (src/sparse_fft_bluestein.cu:7-20): plan buffers and output
+        mem = plan.device_bytes + out.numel() * out.element_size()
+        return SparseFFTResult(out, plan.output_pitch, e0.elapsed_time(e1), mem)
 
 
 def sparse_fft_csc_bluestein_mixed_radix(coo: COOMatrix, u_tile: int = 128) -> SparseFFTResult:

@@ -102,6 +102,11 @@ typedef struct {
                               Bluestein rows in the plan's own allocation
                               (gbsp_execute_to_host then allocates nothing);
                               GBSP_STREAM_TILE_AUTO: reserve them for the automatic tile */
+    int exact_phases;      /* pass-1 twiddles: 0 = default, the entry of the FP64-built table
+                              at the exact integer phase (u*r) mod rows every 4th row and
+                              three-term-recurrence steps (two FMAs) between; 1 = the table
+                              entry at the exact phase for every row (no float products
+                              beyond the table's rounding; slower)                        */
 } gbsp_options;
 
 typedef struct {
@@ -123,6 +128,7 @@ typedef struct {
     int pass1_shape;       /* pass-1 shape in use (1-based)                               */
     int planner;           /* planner that chose the configuration                        */
     int channel_mode;      /* 0 single channel, 1 clusters, 2 sequential channels         */
+    int exact_phases;      /* 1: every pass-1 twiddle an exact table lookup               */
 } gbsp_plan_info;
 
 int         gbsp_version(void);
@@ -213,17 +219,21 @@ int gbsp_column_sums(gbsp_plan_t plan, int u0, int n_rows, void* d_s, size_t s_p
  * (held by every GPU that loads the library until the process exits) and no
  * allocating routine is called.
  *   - The plan's device must be current.  The first call on each device looks
- *     up the array's device address; make that first call before any stream
- *     capture.
+ *     up the array's device address and keeps it; make that first call before
+ *     any stream capture.  The address belongs to the device's context:
+ *     resetting the device (cudaDeviceReset) after that first call is not
+ *     supported.
  *   - Rows of the intermediate are processed in tiles that fit the array; a
  *     plan whose single row would not fit is rejected with
  *     GBSP_ERR_UNSUPPORTED (cannot happen for plans gbsp_plan_create accepts
  *     today: a row is at most a few hundred KB).
  *   - All calls share the array and nothing in it has to start at zero (each
  *     tile is fully rewritten before it is read).  Calls that overlap on the
- *     GPU -- concurrent streams, or several host threads -- race on it:
- *     serialise them.
- * Asynchronous on `stream`, like gbsp_execute. */
+ *     GPU race on it: issue them on one stream, or order their streams with
+ *     events -- calls made one after another on the host but on different
+ *     streams still overlap on the GPU.
+ * Asynchronous on `stream`, like gbsp_execute; read gbsp_plan_error_flags
+ * once the work has finished. */
 int gbsp_execute_noalloc(gbsp_plan_t plan, void* d_out, size_t out_pitch, void* stream);
 
 /* Streams the transform to host memory: the reference's streaming methods
@@ -244,8 +254,20 @@ int gbsp_execute_to_host(gbsp_plan_t plan, void* h_out, size_t out_pitch, int ti
 /* Reads and clears the plan's device error flags (synchronises the device).
  * Bit 0: a bounded wait inside a kernel gave up; bit 1: a stage radix the
  * row kernel was not compiled for (plan/kernel mismatch).  Either way the
- * result of that transform is not valid.  0 means no error was recorded. */
+ * result of that transform is not valid.  0 means no error was recorded.
+ * The asynchronous entry points (gbsp_execute, gbsp_execute_noalloc,
+ * gbsp_batch_execute, gbsp_batch_graph_launch) cannot see the word without
+ * synchronising, so callers read it here once their work has finished; the
+ * blocking ones (gbsp_execute_to_host, gbsp_execute_profiled) and the C++
+ * API of include/sparse_fft.h check it themselves. */
 int gbsp_plan_error_flags(gbsp_plan_t plan, int* flags);
+
+/* Status of a device error word as gbsp_plan_error_flags returns it:
+ * GBSP_OK for 0, else GBSP_ERR_CUDA with gbsp_last_error() naming the bits.
+ * (The reference raises every CUDA failure as an exception,
+ * include/sparse_fft_internal.cuh:16-22; its C++ API here throws on this
+ * status.)  Host-only. */
+int gbsp_device_flags_status(int flags);
 
 /* ---- batches ---------------------------------------------------------------
  * Many matrices of uneven size and sparsity transformed by one persistent

@@ -5,6 +5,10 @@
 // nothing here is a copy of them.  Only tests/ and the golden-fixture script
 // load the resulting oracle/_ref/libref_host.so.
 //
+// The same file compiled with -fatbin gives oracle/_ref/ref_kernels.fatbin:
+// the device code of the included reference translation unit, i.e. the
+// reference's own GPU kernels, which oracle/ref_gpu_driver.cpp launches.
+//
 // Wrapped reference symbols:
 //   read_mtx                    src/mtx_reader.cu:7-77
 //   make_compact_csc            include/sparse_fft_internal.cuh:200-222

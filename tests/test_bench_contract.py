@@ -33,7 +33,7 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference"
     assert d["unit"] == "ms/FFT" and d["higher_is_better"] is False and d["value"] > 0
     assert d["steps"] == 1 and d["n_gpus"] == 1 and d["vs_baseline"] is None
-    assert d["config"]["workload"] == "banded_powerlaw_8219" and d["config"]["shape"] == [8219, 8219]
+    assert d["config"]["workload"] == "uniform_powerlaw_16706" and d["config"]["shape"] == [16706, 16706]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "ms/FFT", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

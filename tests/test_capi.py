@@ -71,3 +71,20 @@ def test_missing_library_raises(monkeypatch, tmp_path):
     monkeypatch.setattr(_capi, "LIB_PATH", tmp_path / "libgbspfft.so")
     with pytest.raises(RuntimeError, match="native library missing"):
         _capi.load(build_if_missing=False)
+
+
+@pytest.mark.parametrize("flags,words", [(1, ["bounded device wait"]), (2, ["not compiled for"]),
+                                         (3, ["bounded device wait", "not compiled for"]), (8, ["unknown bits"])])
+def test_device_error_word_status(flags, words):
+    # the status every synchronous entry point and the C++ API derive from a
+    # plan's device error word (here injected on the host): an error word
+    # other than 0 is a CUDA failure whose message names the bits
+    lib = _capi.load()
+    assert lib.gbsp_device_flags_status(0) == _capi.GBSP_OK
+    assert lib.gbsp_device_flags_status(flags) == _capi.GBSP_ERR_CUDA
+    msg = _capi.last_error()
+    assert f"device error flags {flags}" in msg and "not valid" in msg
+    for w in words:
+        assert w in msg
+    with pytest.raises(gb.GbspError, match="not valid"):
+        _capi.check(lib.gbsp_device_flags_status(flags), "gbsp_execute")

@@ -12,7 +12,18 @@ import pytest
 
 from cuspfft_gb300 import build
 
-REF = Path(os.environ.get("GBSP_REFERENCE_DIR", "/root/reference"))
+
+def reference_dir() -> Path:
+    """GBSP_REFERENCE_DIR, else the tree oracle/build_ref.sh compiled from
+    (recorded in oracle/_ref/REFERENCE_DIR); an empty path when neither is set."""
+    env = os.environ.get("GBSP_REFERENCE_DIR")
+    if env:
+        return Path(env)
+    rec = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "REFERENCE_DIR"
+    return Path(rec.read_text().strip()) if rec.exists() else Path("/nonexistent")
+
+
+REF = reference_dir()
 
 
 @pytest.mark.skipif(not (REF / "src" / "main.cu").exists(), reason="reference sources not present")

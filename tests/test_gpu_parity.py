@@ -294,3 +294,76 @@ def test_wide_matrices_many_channels(cuda, rows, cols):
     check_against_oracle(coo, got)
     with pytest.raises(gb.GbspError):
         gb.Plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, channel_mode=1)
+
+
+@pytest.mark.parametrize("policy,channels", [(gb.GBSP_LEN_3SMOOTH, 4), (gb.GBSP_LEN_7SMOOTH, 5)])
+def test_config_40421_uint32_indices(cuda, policy, channels):
+    # the largest configuration: 40421^2 power-law adjacency, ~351k nnz,
+    # 4-byte row indices (the reference's int32 pass 1,
+    # src/sparse_fft_bluestein.cu:334-364), 6.5 GB output; the convolution
+    # runs as K sequential channels in one CTA per row.  Rows are sampled on
+    # the device; the pad columns of every row are checked there too.
+    import torch
+    coo = synthetic.config_matrix("uniform_powerlaw_40421")
+    g = np.random.default_rng(40421)
+    us = np.unique(np.concatenate([[0, 1, 2, coo.rows // 2, coo.rows // 2 + 1, coo.rows - 1],
+                                   g.integers(0, coo.rows, 14)]))
+    fc = coo.cols // 2 + 1
+    with gb.Plan(coo, length_policy=policy, index_bytes=4) as plan:
+        info = plan.info
+        assert info["index_bytes"] == 4
+        assert info["channels"] == channels and info["channel_mode"] == 2
+        out = plan.empty_output()
+        out.fill_(complex(7.0, 7.0))
+        plan.execute(out)
+        torch.cuda.synchronize()
+        assert plan.error_flags() == 0
+        got = out[torch.as_tensor(us, device=out.device)].cpu().numpy()
+        assert bool((out[:, fc:] == 0).all())
+        del out
+    ref = fp64.spectrum_rows_fp64(coo.rows, coo.cols, coo.row_idx, coo.col_idx, us)
+    err = fp64.rel_l2(got[:, :fc], ref)
+    assert err <= REL_L2_TOL, f"rel-L2 {err:.3e}"
+
+
+@pytest.mark.parametrize("name", ["uniform_3001x2048", "banded_powerlaw_8219"])
+def test_exact_phase_mode(cuda, name):
+    # exact_phases=1: every pass-1 twiddle is the FP64-built table entry at its
+    # exact integer phase (u*r) mod rows; the default reads the table every
+    # 4th row and steps the recurrence between.  Both within 1e-5 of FP64,
+    # with and without Kahan compensation.
+    coo = synthetic.config_matrix(name)
+    us = None if coo.rows < 4000 else np.unique(np.r_[0, 1, 2, 3, 4, 5, 31, 32, 33, coo.rows // 2, coo.rows - 1])
+    errs = {}
+    for exact in (0, 1):
+        for kahan in (0, -1):
+            got, info = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, exact_phases=exact,
+                                 kahan_min_degree=kahan)
+            assert info["exact_phases"] == exact
+            errs[exact, kahan] = check_against_oracle(coo, got, us=us)
+    print(name, {k: f"{v:.3e}" for k, v in errs.items()})
+
+
+@pytest.mark.parametrize("rows,cols,index_bytes", [(24001, 40, 0), (70001, 64, 0)])
+def test_exact_phase_mode_tall(cuda, rows, cols, index_bytes):
+    # half table (24001 rows) and two-level table with 64-bit phases (70001)
+    g = np.random.default_rng(rows + 1)
+    n = 2 * rows
+    coo = synthetic.normalise(rows, cols, g.integers(0, rows, n), g.integers(0, cols, n))
+    got, info = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, exact_phases=1, index_bytes=index_bytes)
+    us = np.unique(np.r_[0:5, rows // 2 - 1:rows // 2 + 2, rows - 3:rows] % rows)
+    check_against_oracle(coo, got, us=us)
+
+
+def test_exact_phase_mode_batch(cuda):
+    import torch
+    mats = [synthetic.uniform_matrix(r, c, n, seed=r) for r, c, n in [(501, 300, 4000), (1301, 977, 20000),
+                                                                        (64, 2000, 900)]]
+    with gb.Batch(mats, exact_phases=1) as batch:
+        outs = batch.empty_outputs()
+        batch.set_outputs(outs)
+        batch.execute()
+        torch.cuda.synchronize()
+        assert batch.error_flags() == 0
+        for coo, out in zip(mats, outs):
+            check_against_oracle(coo, out.cpu().numpy())
