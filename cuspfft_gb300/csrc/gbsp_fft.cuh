@@ -309,11 +309,15 @@ template <int P> struct Radix<P, false> {
 //   MODE 0: forward DIF stage
 //   MODE 1: inverse DIT stage
 //   MODE 2: last forward stage + pointwise filter multiply + first inverse
-//           stage (their twiddles cancel, so neither is applied)
+//           stage (their twiddles cancel, so neither is applied); the last
+//           stage always has span 1, so butterfly t covers buf[t*R, t*R+R)
 // Twiddles are stored q-major per stage, tw[(q-1)*m + k] = W_{R*m}^{q*k}, so a
-// warp's loads for one q are contiguous.  The filter of the fused stage (the
-// last stage, m = 1, base = t*R) is stored in the same thread order,
-// filt[q*(Lp/R) + t].
+// warp's loads for one q are contiguous.  TWG: the twiddles are read through
+// the read-only global path (stage 0, whose table does not fit in shared
+// memory beside the row), else from shared memory.  The entries at k = 0 are
+// exactly 1, so every butterfly applies its twiddles without a branch (a
+// complex product by (1, 0) is exact).  The filter of the fused stage is
+// stored in the same thread order, filt[q*(Lp/R) + t], in global memory.
 //
 // Thread -> butterfly mapping: for spans m >= 16 consecutive threads take
 // consecutive k (unit-stride shared-memory accesses); for shorter spans with
@@ -324,12 +328,34 @@ __host__ __device__ constexpr bool stage_j_fastest(int R, int m, int l) {
     return m > 1 && m < 16 && l > 1 && ((R * m) & 1) == 1;
 }
 
-template <int R, int MODE, typename V>
+template <bool TWG, typename V>
+__device__ __forceinline__ V tw_load(const V* __restrict__ p) {
+    if constexpr (TWG) return __ldg(p);
+    else return *p;
+}
+
+template <int R, int MODE, bool TWG, typename V>
 __device__ __forceinline__ void fft_stage(V* __restrict__ buf, int Lp, int m, uint32_t magic,
                                           const V* __restrict__ tw, const V* __restrict__ filt,
                                           int tid, int nthreads) {
     using RX = Radix<R>;
     const int nb = Lp / R;
+    if constexpr (MODE == 2) {
+        for (int t = tid; t < nb; t += nthreads) {
+            V* p = buf + t * R;
+            V a[R];
+#pragma unroll
+            for (int s = 0; s < R; s++) a[s] = p[s];
+            RX::fwd(a);
+            const V* f = filt + t;
+#pragma unroll
+            for (int q = 0; q < R; q++) a[RX::out_reg(q)] = cmul(a[RX::out_reg(q)], __ldg(f + q * nb));
+            RX::inv(a);
+#pragma unroll
+            for (int s = 0; s < R; s++) p[s] = a[s];
+        }
+        return;
+    }
     const int l = nb / m;
     const bool jfast = stage_j_fastest(R, m, l);
     for (int t = tid; t < nb; t += nthreads) {
@@ -338,15 +364,15 @@ __device__ __forceinline__ void fft_stage(V* __restrict__ buf, int Lp, int m, ui
         else if (!jfast) { j = (int)__umulhi((uint32_t)t, magic); k = t - j * m; }
         else { k = (int)__umulhi((uint32_t)t, magic); j = t - k * l; }
         const int base = j * R * m + k;
+        const V* twk = tw + k;
         V a[R];
         if (MODE == 1) {
             // inputs q sit in register out_reg(q)
 #pragma unroll
             for (int q = 0; q < R; q++) a[RX::out_reg(q)] = buf[base + q * m];
-            if (k != 0) {
 #pragma unroll
-                for (int q = 1; q < R; q++) a[RX::out_reg(q)] = cmulc(a[RX::out_reg(q)], tw[(q - 1) * m + k]);
-            }
+            for (int q = 1; q < R; q++)
+                a[RX::out_reg(q)] = cmulc(a[RX::out_reg(q)], tw_load<TWG>(twk + (q - 1) * m));
             RX::inv(a);
 #pragma unroll
             for (int s = 0; s < R; s++) buf[base + s * m] = a[s];
@@ -354,20 +380,11 @@ __device__ __forceinline__ void fft_stage(V* __restrict__ buf, int Lp, int m, ui
 #pragma unroll
             for (int s = 0; s < R; s++) a[s] = buf[base + s * m];
             RX::fwd(a);
-            if (MODE == 0) {
-                if (k != 0) {
 #pragma unroll
-                    for (int q = 1; q < R; q++) a[RX::out_reg(q)] = cmul(a[RX::out_reg(q)], tw[(q - 1) * m + k]);
-                }
+            for (int q = 1; q < R; q++)
+                a[RX::out_reg(q)] = cmul(a[RX::out_reg(q)], tw_load<TWG>(twk + (q - 1) * m));
 #pragma unroll
-                for (int q = 0; q < R; q++) buf[base + q * m] = a[RX::out_reg(q)];
-            } else {
-#pragma unroll
-                for (int q = 0; q < R; q++) a[RX::out_reg(q)] = cmul(a[RX::out_reg(q)], filt[q * nb + t]);
-                RX::inv(a);
-#pragma unroll
-                for (int s = 0; s < R; s++) buf[base + s * m] = a[s];
-            }
+            for (int q = 0; q < R; q++) buf[base + q * m] = a[RX::out_reg(q)];
         }
     }
 }
@@ -388,14 +405,14 @@ constexpr int MAX_RADIX_NT512 = 40;
 // Runs one stage of radix R; returns false (and touches nothing) when this
 // kernel was not compiled for R, so a plan/kernel mismatch is reported
 // instead of silently skipping the stage.
-template <int MODE, int MAXR, typename V>
+template <int MODE, int MAXR, bool TWG, typename V>
 __device__ __forceinline__ bool fft_stage_dispatch(int R, V* buf, int Lp, int m, uint32_t magic,
                                                    const V* tw, const V* filt, int tid, int nthreads) {
     switch (R) {
 #define GBSP_STAGE_CASE(r)                                                                   \
         case r:                                                                              \
             if constexpr (r <= MAXR) {                                                       \
-                fft_stage<r, MODE>(buf, Lp, m, magic, tw, filt, tid, nthreads);              \
+                fft_stage<r, MODE, TWG>(buf, Lp, m, magic, tw, filt, tid, nthreads);         \
                 return true;                                                                 \
             }                                                                                \
             return false;

@@ -511,10 +511,10 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     const int half_slots = (int)(a.out_pitch >> 1);
     const int hc = cols / 2;
     const int cols_even = (cols + 1) & ~1;
-    // stage 0 twiddles stream from global memory, the rest sit in shared memory
-    auto tw_of = [&](int s) -> const float2* {
-        return (s == 0) ? a.fft_tw + fd.twoff[0] : twr + (fd.twoff[s] - fd.rest_base);
-    };
+    // stage 0 twiddles stream from global memory (read-only path), the rest
+    // sit in shared memory
+    const float2* tw0 = a.fft_tw + fd.twoff[0];
+    auto tw_smem = [&](int s) -> const float2* { return twr + (fd.twoff[s] - fd.rest_base); };
     const int u = a.u0 + t;
     const float2* srow = a.S + (size_t)t * a.s_pitch;
     bool ok = true;
@@ -579,16 +579,25 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
         }
         // forward DIF, filter multiply fused with the last stage, inverse DIT
         const int S1 = fd.nst - 1;
-        for (int s = 0; s < S1; s++) {
-            ok &= fft_stage_dispatch<0, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                              (const float2*)nullptr, tid, nt);
+        const float2* none = nullptr;
+        if (S1 > 0) {
+            ok &= fft_stage_dispatch<0, MAXR, true>(fd.R[0], buf, Lp, fd.m[0], fd.magic[0], tw0, none, tid, nt);
             __syncthreads();
         }
-        ok &= fft_stage_dispatch<2, MAXR>(fd.R[S1], buf, Lp, fd.m[S1], fd.magic[S1], tw_of(S1), filtq, tid, nt);
+        for (int s = 1; s < S1; s++) {
+            ok &= fft_stage_dispatch<0, MAXR, false>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_smem(s), none,
+                                                     tid, nt);
+            __syncthreads();
+        }
+        ok &= fft_stage_dispatch<2, MAXR, false>(fd.R[S1], buf, Lp, 1, 0u, none, filtq, tid, nt);
         __syncthreads();
-        for (int s = S1 - 1; s >= 0; s--) {
-            ok &= fft_stage_dispatch<1, MAXR>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_of(s),
-                                              (const float2*)nullptr, tid, nt);
+        for (int s = S1 - 1; s >= 1; s--) {
+            ok &= fft_stage_dispatch<1, MAXR, false>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_smem(s), none,
+                                                     tid, nt);
+            __syncthreads();
+        }
+        if (S1 > 0) {
+            ok &= fft_stage_dispatch<1, MAXR, true>(fd.R[0], buf, Lp, fd.m[0], fd.magic[0], tw0, none, tid, nt);
             __syncthreads();
         }
         if (SEQ && qc < K - 1) {  // park the channel for the combine
@@ -647,7 +656,71 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                 __stcs(dst, make_float4(o0.x, o0.y, o1.x, o1.y));
             }
         }
+    } else if constexpr (SEQ) {
+        // Sequential channels: channels 0..K-2 wait in this CTA's scratch
+        // (global memory, L2-resident), channel K-1 is in buf.  Each thread
+        // takes WS slots per pass and, channel by channel, issues all of the
+        // slots' loads (parked values and post chirps from L2) before any
+        // product, so the L2 latency is paid once per channel and WS slots
+        // rather than once per value.  The channels are summed in order.
+        constexpr int WS = 4;
+        const float2* zs0 = a.zscratch + (size_t)blockIdx.x * (K - 1) * Lp;
+        for (int s0 = lo + tid; s0 < hi; s0 += WS * nt) {
+            int cc[WS][2], nn[WS][2];
+            float2 acc[WS][2];
+#pragma unroll
+            for (int w = 0; w < WS; w++) {
+                const int s = s0 + w * nt;
+                const int sel = s >= half_slots;
+                const int v = 2 * (s - sel * half_slots);
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int vv = v + e;
+                    const int c = (s >= hi || vv > hc) ? -1 : sel ? (vv == 0 ? 0 : cols - vv) : vv;
+                    int n = c < 0 ? 0 : c;
+                    while (n >= Lp) n -= Lp;  // cols <= (K/2 + 1) * Lp: a few steps at most
+                    cc[w][e] = c < 0 ? 0 : c;
+                    nn[w][e] = n;
+                    acc[w][e] = make_float2(0.f, 0.f);
+                }
+            }
+            for (int qq = 0; qq < K; qq++) {
+                const float2* pq = a.post + (size_t)qq * cols;
+                const float2* zq = zs0 + (size_t)qq * Lp;
+                const bool last = qq == K - 1;
+                float2 pv[WS][2], zv[WS][2];
+#pragma unroll
+                for (int w = 0; w < WS; w++)
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        pv[w][e] = __ldg(pq + cc[w][e]);
+                        zv[w][e] = last ? buf[nn[w][e]] : __ldcg(zq + nn[w][e]);
+                    }
+#pragma unroll
+                for (int w = 0; w < WS; w++)
+#pragma unroll
+                    for (int e = 0; e < 2; e++) acc[w][e] = cadd(acc[w][e], cmul(zv[w][e], pv[w][e]));
+            }
+#pragma unroll
+            for (int w = 0; w < WS; w++) {
+                const int s = s0 + w * nt;
+                if (s >= hi) break;
+                const int sel = s >= half_slots;
+                const int v = 2 * (s - sel * half_slots);
+                float2 o0 = (v > hc) ? make_float2(0.f, 0.f) : acc[w][0];
+                float2 o1 = (v + 1 > hc) ? make_float2(0.f, 0.f) : acc[w][1];
+                if (sel) {
+                    o0.y = -o0.y;
+                    o1.y = -o1.y;
+                }
+                const int row = sel ? u2 : u;
+                const int drow = row < a.map_split ? row - a.map_lo : row - a.map_hi;
+                float4* dst = reinterpret_cast<float4*>(a.out + (size_t)drow * a.out_pitch + v);
+                __stcs(dst, make_float4(o0.x, o0.y, o1.x, o1.y));
+            }
+        }
     } else {
+        // clusters: the K channels sit in the shared memories of the cluster
         for (int s = lo + tid; s < hi; s += nt) {
             const int sel = s >= half_slots;
             const int v = 2 * (s - sel * half_slots);
@@ -660,16 +733,8 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                     const int c = sel ? (vv == 0 ? 0 : cols - vv) : vv;
                     int n = c;
                     while (n >= Lp) n -= Lp;
-                    if constexpr (MODE == ROW_SEQW) {
-                        // channels 0..K-2 wait in this CTA's scratch, K-1 in buf
-                        const float2* zs = a.zscratch + (size_t)blockIdx.x * (K - 1) * Lp + n;
-                        for (int qq = 0; qq < K - 1; qq++)
-                            val = cadd(val, cmul(zs[(size_t)qq * Lp], __ldg(a.post + (size_t)qq * cols + c)));
-                        val = cadd(val, cmul(buf[n], __ldg(a.post + (size_t)(K - 1) * cols + c)));
-                    } else {
-                        for (int qq = 0; qq < K; qq++)
-                            val = cadd(val, cmul(zsrc[qq][n], __ldg(a.post + (size_t)qq * cols + c)));
-                    }
+                    for (int qq = 0; qq < K; qq++)
+                        val = cadd(val, cmul(zsrc[qq][n], __ldg(a.post + (size_t)qq * cols + c)));
                     if (sel) val.y = -val.y;
                 }
                 o[e] = val;
@@ -698,7 +763,9 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
 
     constexpr int MAXR = (NTMAX > 512) ? MAX_RADIX_NT1024 : MAX_RADIX_NT512;
     int q = 0, cid = blockIdx.x, ncl = gridDim.x;
-    const float2* zsrc[(MODE == ROW_CLUSTER || MODE == ROW_SEQ) ? MAX_CHANNELS : 1];
+    // the channels' shared-memory buffers across a cluster (ROW_CLUSTER);
+    // the other modes read their channels from buf and the scratch directly
+    const float2* zsrc[MODE == ROW_CLUSTER ? MAX_CHANNELS : 1];
     if constexpr (MODE == ROW_CLUSTER) {
         const int K = a.K;
         cg::cluster_group cl = cg::this_cluster();
@@ -708,13 +775,6 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
 #pragma unroll
         for (int i = 0; i < MAX_CHANNELS; i++)
             zsrc[i] = (i < K) ? cl.map_shared_rank(buf, i) : buf;
-    } else if constexpr (MODE == ROW_SEQ) {
-        // channels 0..K-2 wait in this CTA's scratch, K-1 in buf (K > MAX_CHANNELS
-        // computes the pointers as it goes)
-        const int K = a.K;
-#pragma unroll
-        for (int i = 0; i < MAX_CHANNELS; i++)
-            zsrc[i] = (i < K - 1) ? a.zscratch + ((size_t)blockIdx.x * (K - 1) + i) * fd.Lp : buf;
     } else {
         zsrc[0] = buf;
     }
