@@ -350,6 +350,24 @@ def run_batched(args, torch, gb, synthetic) -> dict:
         "learned_regret_heldout": meta.get("regret_learned"), "analytic_regret_heldout": meta.get("regret_analytic"),
     }
     batch.close()
+    # context: the reference's own GPU method (cuFFT smooth, its kernels on
+    # this device) run matrix by matrix, as its driver does
+    # (src/main.cu:486-524): the sum of its tile-loop times over the batch
+    from oracle import refgpu
+    if refgpu.available():
+        ref_ms = {}
+        for ut in (128, 1024):
+            tot = 0.0
+            for m in mats:
+                _, t = refgpu.run(m.rows, m.cols, m.row_idx, m.col_idx, 7, u_tile=ut, n_times=1)
+                tot += t[0]
+            ref_ms[ut] = tot
+        res["reference_method_per_matrix"] = {
+            "method": "sparse_fft_csc_bluestein_cufft_smooth (the reference's kernels and cuFFT on this GB300), "
+                      "one call per matrix, tile loops summed",
+            "matrices_per_s_u_tile_128": round(64e3 / ref_ms[128], 1),
+            "matrices_per_s_u_tile_1024": round(64e3 / ref_ms[1024], 1),
+            "batched_speedup_vs_it": round(min(ref_ms.values()) / ms_b, 2)}
     # supplementary: small matrices, where the batched form's launch savings dominate
     small = small_matrices(synthetic)
     sb, sp, sbatch = batch_vs_plain(args, torch, gb, small)

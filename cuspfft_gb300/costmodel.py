@@ -37,7 +37,7 @@ from . import synthetic, tuning
 DATA_DIR = Path(__file__).resolve().parent / "data"
 DEFAULT_MODEL = DATA_DIR / "cost_model.npz"
 DEFAULT_DATA = DATA_DIR / "tune_timings.npz"
-MAX_R, MAX_P = 8, 6
+MAX_R, MAX_P = 8, 8
 N_M, N_R, N_P = 18, 10, 8
 H = GBSP_MLP_HIDDEN
 

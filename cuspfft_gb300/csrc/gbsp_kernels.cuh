@@ -334,7 +334,7 @@ __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage,
     }
     __syncthreads();
     const int ncol = min(cw, a.s_cols - c0);
-    const int cw_log2 = __ffs(cw) - 1;  // every pass-1 shape's window is 32 or 64 columns
+    const int cw_log2 = __ffs(cw) - 1;  // every pass-1 shape's window is 16, 32 or 64 columns
     for (int e = threadIdx.x; e < UBLK * cw; e += blockDim.x) {
         const int row = e >> cw_log2, lc = e & (cw - 1);
         const int ul = ul0 + row;

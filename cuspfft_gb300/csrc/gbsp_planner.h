@@ -46,8 +46,7 @@ extern const P1Shape kP1Shapes[N_P1_SHAPES];
 size_t row_table_entries(int tab, int rows);
 size_t p1_smem_bytes(const P1Shape& sh, int rows);
 // Indices (0-based, preference order) of the shapes that fit for `rows`
-// under the table mode (0 auto, 1 full, 2 half, 3 two-level).  Auto offers
-// the two-level shapes only when no full or half table fits.
+// under the table mode (0 auto, 1 full, 2 half, 3 two-level).
 std::vector<int> fitting_p1_shapes(int rows, size_t smem_cap, int table_mode);
 
 // Shared memory per CTA available to the kernels: the current device's

@@ -14,7 +14,7 @@ namespace gbsp {
 // The CSC half of a plan's build, one launch:
 //
 // Blocks [0, task_blocks): the pass-1 task tables, one warp per window of cw
-// (32 or 64) columns.  The window's active columns are found in sparse_cols
+// (16, 32 or 64) columns.  The window's active columns are found in sparse_cols
 // (strictly increasing) by a binary search for its first column.  With
 // T = max(32, ceil(window nonzeros / P1_WARPS)), column lc splits into
 // np = ceil(deg / T) tasks at nonzero offsets floor(k * deg / np); the tasks
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(SETUP_WARPS * 32) k_csc_setup(CscSetupArgs a) 
     const int w = blockIdx.x * SETUP_WARPS + wl;
     if (w >= a.n_win) return;  // warp-uniform
     const int cw = a.cw, vmax = p1_vmax(cw);
-    const int halves = cw / 32;  // columns lane and lane + 32
+    const int halves = (cw + 31) / 32;  // columns lane and lane + 32; lanes >= cw idle when cw = 16
     const int c0 = w * cw;
     // first active column >= c0
     int lo = 0, hi = a.n_active;
@@ -101,7 +101,8 @@ __global__ void __launch_bounds__(SETUP_WARPS * 32) k_csc_setup(CscSetupArgs a) 
     }
     const int nt = base;
     uint8_t* s0 = a.slot0 + (size_t)w * (cw + 1);
-    for (int h = 0; h < halves; h++) s0[h * 32 + lane] = (uint8_t)min(first[h], vmax);
+    for (int h = 0; h < halves; h++)
+        if (h * 32 + lane < cw) s0[h * 32 + lane] = (uint8_t)min(first[h], vmax);
     if (lane == 0) s0[cw] = (uint8_t)min(nt, vmax);
     if (nt > vmax) {
         if (lane == 0) atomicOr(a.bad, 2);

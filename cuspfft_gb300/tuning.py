@@ -23,7 +23,7 @@ from .sparse_fft import COOMatrix, CompactCSC, _ip, _stream_handle, make_compact
 F_MATRIX = slice(0, 18)
 F_ROWS = slice(18, 28)
 F_PASS1 = slice(28, 36)
-MAX_CANDIDATES = 8 * 6
+MAX_CANDIDATES = 8 * 8  # row choices x pass-1 shapes (GBSP_N_PASS1_SHAPES)
 
 
 def candidates(rows: int, cols: int, base: Optional[GbspOptions] = None, max_rows_cands: int = 8,

@@ -59,9 +59,11 @@ enum { GBSP_PLANNER_MODEL = 0, GBSP_PLANNER_LEARNED = 1 };
 
 /* Pass-1 shapes (gbsp_options.pass1_shape, 1-based):
  *   1: 256 rows x 32-column windows, full twiddle table
- *   2: 256 x 32, half table      3: 128 x 64, full    4: 128 x 32, full
- *   5: 128 x 64, half            6: 128 x 32, half
- *   7: 256 x 32, two-level       8: 128 x 32, two-level (tall matrices) */
+ *   2: 256 x 32, half table      3: 128 x 64, full    4: 256 x 16, full
+ *   5: 256 x 16, half            6: 128 x 32, half
+ *   7: 256 x 32, two-level       8: 128 x 32, two-level (tall matrices)
+ * The automatic choice takes the first that fits of 1, 2, 7, 3, 4, 5, 6, 8
+ * (measured on GB300); the tuner and the learned planner consider them all. */
 #define GBSP_N_PASS1_SHAPES 8
 /* Length of the cost-model feature vector (gbsp_plan_features). */
 #define GBSP_N_FEATURES 36
@@ -88,7 +90,7 @@ typedef struct {
                               in [64, 1024] (at most 512 when a radix exceeds 16)         */
     int row_table_mode;    /* pass-1 twiddle table: 0 = auto, 1 = full circle,
                               2 = half circle, 3 = two-level (W^p = hi[p/256]*lo[p%256],
-                              any row count; auto uses it only when no other fits)       */
+                              any row count)                                              */
     int radix[8];          /* channel FFT radix per stage, first to last, 0-terminated;
                               all zero = auto.  Allowed: 2 3 4 5 7 8 9 12 15 16 20 21
                               24 25 28 32 35 40; product = channel length                 */

@@ -13,7 +13,7 @@ from oracle import mlp as mlp_oracle
 
 def test_candidates_cross_product():
     cands, nr, npp = tuning.candidates(8219, 8219, length_policy=gb.GBSP_LEN_7SMOOTH)
-    assert nr == 8 and npp == 6 and len(cands) == 48
+    assert nr == 8 and npp == 8 and len(cands) == 64  # every shape fits 8219 rows
     for i in range(nr):
         for j in range(npp):
             c = cands[i * npp + j]
@@ -25,9 +25,12 @@ def test_candidates_cross_product():
         tuning.candidates(8219, 8219, length_policy=gb.GBSP_LEN_7SMOOTH, pass1_shape=9)
 
 
-def test_candidates_large_rows_use_half_table():
+def test_candidates_large_rows_prefer_two_level_table():
+    # 40421 rows: neither a full nor a half table fits beside 256-row items;
+    # the two-level table does (measured faster than 128-row items with the
+    # half table), the half-table and two-level 128-row shapes follow
     cands, nr, npp = tuning.candidates(40421, 40421, length_policy=gb.GBSP_LEN_7SMOOTH)
-    assert npp == 1 and cands[0].pass1_shape == 6  # 128 x 32 windows, half table
+    assert npp == 3 and [c.pass1_shape for c in cands[:3]] == [7, 6, 8]
     assert all(int(np.prod(c.radices())) * 5 == 81000 for c in cands)
 
 
