@@ -75,6 +75,8 @@ def parse():
                     help="timed transforms of the 40421^2 workload (0 skips it)")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference's GPU methods")
     ap.add_argument("--no-precision-modes", action="store_true")
+    ap.add_argument("--rows", type=int, default=0,
+                    help="keep only the workload's first N rows (a smaller case of the same kernels, for profiling)")
     return ap.parse_args()
 
 
@@ -402,8 +404,12 @@ def main():
     peaks = measured_peaks()
 
     coo = synthetic.config_matrix(args.workload)
+    if args.rows > 0:
+        keep = coo.row_idx < args.rows
+        coo = gb.COOMatrix(min(args.rows, coo.rows), coo.cols, coo.row_idx[keep], coo.col_idx[keep])
     csc = gb.make_compact_csc(coo)
-    plan = gb.Plan(coo, length_policy=args.policy, u_tile=args.u_tile, csc=csc)
+    idx_bytes = 4 if args.workload == "uniform_powerlaw_40421" else 0  # the configuration's uint32 indices
+    plan = gb.Plan(coo, length_policy=args.policy, u_tile=args.u_tile, csc=csc, index_bytes=idx_bytes)
     info = plan.info
     out = plan.empty_output()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
@@ -492,7 +498,7 @@ def main():
         for s in range(args.e2e_steps + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            with gb.Plan(coo, length_policy=args.policy, csc=pin_csc, u_tile=1024,
+            with gb.Plan(coo, length_policy=args.policy, csc=pin_csc, u_tile=1024, index_bytes=idx_bytes,
                          stream_tile_rows=gb.GBSP_STREAM_TILE_AUTO) as p2plan:
                 p2plan.execute_to_host(host_out)
             if s > 0:
@@ -552,7 +558,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": args.workload, "description": WORKLOADS[args.workload],
+            "config": {"workload": args.workload + (f" (first {coo.rows} rows)" if args.rows else ""),
+                       "description": WORKLOADS[args.workload],
                        "shape": [coo.rows, coo.cols], "nnz": coo.nnz,
                        "method": "sparse_fft_csc_bluestein_cufft_smooth" if args.policy == 7
                        else "sparse_fft_csc_bluestein_mixed_radix",
