@@ -545,8 +545,8 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                 float2 acc = make_float2(0.f, 0.f);
                 for (int c = n; c < cols; c += 2 * Lp) {
                     const int c2 = c + Lp;
-                    const float2 x0 = __ldcs(srow + c), p0 = __ldg(preq + c);
-                    const float2 x1 = (c2 < cols) ? __ldcs(srow + c2) : make_float2(0.f, 0.f);
+                    const float2 x0 = __ldcg(srow + c), p0 = __ldg(preq + c);
+                    const float2 x1 = (c2 < cols) ? __ldcg(srow + c2) : make_float2(0.f, 0.f);
                     const float2 p1 = (c2 < cols) ? __ldg(preq + c2) : make_float2(0.f, 0.f);
                     acc = cadd(acc, cadd(cmul(x0, p0), cmul(x1, p1)));
                 }
@@ -555,7 +555,10 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
             __syncthreads();
         } else if constexpr (MULTI) {
             // Several input columns fold onto one slot: slot n gets
-            // sum_j pre[n + j*Lp] * x[n + j*Lp].  Each thread owns its slots, so
+            // sum_j pre[n + j*Lp] * x[n + j*Lp].  Every channel reads the whole
+            // S row, so it is loaded to stay in L2 for the next channel (an
+            // evict-first load made each channel re-read it from DRAM).
+            // Each thread owns its slots, so
             // no zero fill or barrier between sections; all of a slot's loads
             // are issued before its products.
             // L = K*Lp >= 2*cols - 1 gives cols/Lp <= K/2 + 1/(2Lp): at most
@@ -567,7 +570,7 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                 for (int j = 0; j < MAXSEC; j++) {
                     const int c = n + j * Lp;
                     const bool ok = c < cols;
-                    xv[j] = ok ? __ldcs(srow + c) : make_float2(0.f, 0.f);
+                    xv[j] = ok ? __ldcg(srow + c) : make_float2(0.f, 0.f);
                     pv[j] = ok ? __ldg(preq + c) : make_float2(0.f, 0.f);
                 }
                 float2 acc = make_float2(0.f, 0.f);
