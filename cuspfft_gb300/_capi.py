@@ -58,6 +58,7 @@ class GbspOptions(C.Structure):
         ("channel_mode", C.c_int),
         ("stream_tile_rows", C.c_int),
         ("exact_phases", C.c_int),
+        ("force_bluestein", C.c_int),
     ]
 
     def radices(self) -> tuple:
@@ -72,7 +73,7 @@ class GbspPlanInfo(C.Structure):
         ("output_pitch", C.c_int), ("half_rows", C.c_int), ("u_tile", C.c_int),
         ("index_bytes", C.c_int), ("row_table_mode", C.c_int), ("rows_threads", C.c_int),
         ("device_bytes", C.c_size_t), ("pass1_shape", C.c_int), ("planner", C.c_int), ("channel_mode", C.c_int),
-        ("exact_phases", C.c_int),
+        ("exact_phases", C.c_int), ("direct", C.c_int),
     ]
 
     def as_dict(self) -> dict:

@@ -483,6 +483,10 @@ struct RowsArgs {
     // ROW_SEQ: per-CTA scratch for the first K-1 channels of a row,
     // (K-1) x Lp complex per CTA, CTA b at zscratch + b*(K-1)*Lp
     float2* zscratch;
+    // direct plans (cols smooth: one forward FFT of length cols instead of
+    // the Bluestein convolution): drev[c] = where the forward network leaves
+    // frequency c; nullptr for Bluestein plans
+    const int* drev;
 };
 
 // How the K channels of a long row are laid out on the GPU.
@@ -498,7 +502,9 @@ constexpr int ROW_SINGLE = 0, ROW_CLUSTER = 1, ROW_SEQ = 2, ROW_SEQW = 3;
 // One Bluestein row t of the tile (u = u0 + t), channel q of K: input,
 // forward network, filter, inverse network, Hermitian-paired output.  Whole
 // CTA (with the cluster when K > 1); ends on a barrier, so the next row may
-// overwrite buf at once.
+// overwrite buf at once.  Direct plans (a.drev set, K = 1) run only the
+// forward network over the row's cols points and gather the spectrum through
+// drev in the writer.
 template <int MAXR, int MODE>
 __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& fd, int t, int q, float2* buf,
                                               const float2* twr, const float2* const* zsrc, uint64_t* bar,
@@ -517,6 +523,7 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     auto tw_smem = [&](int s) -> const float2* { return twr + (fd.twoff[s] - fd.rest_base); };
     const int u = a.u0 + t;
     const float2* srow = a.S + (size_t)t * a.s_pitch;
+    const bool direct = !MULTI && a.drev != nullptr;
     bool ok = true;
     // ROW_SEQ runs every channel of the row here; the other modes one
     const int q_end = SEQ ? K : q + 1;
@@ -583,15 +590,19 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
         // forward DIF, filter multiply fused with the last stage, inverse DIT
         const int S1 = fd.nst - 1;
         const float2* none = nullptr;
-        if (S1 > 0) {
+        // (a direct plan runs the forward network alone, its last stage --
+        // span 1, twiddles exactly 1 -- included: X in digit-reversed order)
+        const int S_fwd = direct ? S1 + 1 : S1;
+        if (S_fwd > 0) {
             ok &= fft_stage_dispatch<0, MAXR, true>(fd.R[0], buf, Lp, fd.m[0], fd.magic[0], tw0, none, tid, nt);
             __syncthreads();
         }
-        for (int s = 1; s < S1; s++) {
+        for (int s = 1; s < S_fwd; s++) {
             ok &= fft_stage_dispatch<0, MAXR, false>(fd.R[s], buf, Lp, fd.m[s], fd.magic[s], tw_smem(s), none,
                                                      tid, nt);
             __syncthreads();
         }
+        if (direct) continue;
         ok &= fft_stage_dispatch<2, MAXR, false>(fd.R[S1], buf, Lp, 1, 0u, none, filtq, tid, nt);
         __syncthreads();
         for (int s = S1 - 1; s >= 1; s--) {
@@ -637,8 +648,13 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
                     const int vv = v + e;
                     const int c = (s >= hi || vv > hc) ? -1 : sel ? (vv == 0 ? 0 : cols - vv) : vv;
                     col[w][e] = c;
-                    pv[w][e] = (c >= 0) ? __ldg(a.post + c) : make_float2(0.f, 0.f);
-                    zv[w][e] = buf[c < 0 ? 0 : c];
+                    if (direct) {  // F[u][c] = X[c], no chirp; (1, 0) keeps the product exact
+                        pv[w][e] = make_float2(1.f, 0.f);
+                        zv[w][e] = buf[c < 0 ? 0 : __ldg(a.drev + c)];
+                    } else {
+                        pv[w][e] = (c >= 0) ? __ldg(a.post + c) : make_float2(0.f, 0.f);
+                        zv[w][e] = buf[c < 0 ? 0 : c];
+                    }
                 }
             }
 #pragma unroll
@@ -760,7 +776,7 @@ __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc
     extern __shared__ float4 smem_raw[];
     __shared__ uint64_t in_bar;
     float2* buf = reinterpret_cast<float2*>(smem_raw);
-    float2* twr = buf + fd.Lp;
+    float2* twr = buf + row_buf_len(fd.Lp);
     for (int i = threadIdx.x; i < fd.rest_len; i += blockDim.x) twr[i] = a.fft_tw[fd.rest_base + i];
     if (threadIdx.x == 0) mbar_init(&in_bar, 1);
 
@@ -843,7 +859,7 @@ k_bluestein_rows_batch(const RowsBatch* __restrict__ descs, const long* __restri
         if (m != loaded) {
             if (threadIdx.x == 0) cur = descs[m];
             __syncthreads();
-            twr = buf + cur.fd.Lp;
+            twr = buf + row_buf_len(cur.fd.Lp);
             for (int i = threadIdx.x; i < cur.fd.rest_len; i += blockDim.x)
                 twr[i] = cur.a.fft_tw[cur.fd.rest_base + i];
             __syncthreads();

@@ -26,6 +26,10 @@ GBSP_HD constexpr int p1_pitch(int cw) { return p1_vmax(cw) + 1; }
 GBSP_HD constexpr size_t p1_head_bytes(int ku, int cw) {
     return (size_t)32 * ku * p1_pitch(cw) * 8 + (size_t)P1_WARPS * 32 * 16;
 }
+// complex slots of the row kernel's shared-memory row buffer for a channel of
+// Lp points: rounded up to even, so the bulk copy of an odd-length row (which
+// moves whole 16-byte pairs) stays inside the buffer
+GBSP_HD constexpr int row_buf_len(int Lp) { return (Lp + 1) & ~1; }
 // pass-1 twiddle table layouts (see row_twiddle)
 constexpr int TAB_FULL = 0, TAB_HALF = 1, TAB_TWO = 2;
 constexpr int TWO_LO_BITS = 8, TWO_LO = 1 << TWO_LO_BITS;

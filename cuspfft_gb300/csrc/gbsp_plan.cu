@@ -38,6 +38,8 @@ struct gbsp_plan_s {
     int half_rows = 0, u_tile = 0, out_cols = 0, out_pitch = 0;
     int idx_bytes = 2, tab_mode = 0, big = 0, kahan_min = 64, ntab = 0;  // tab_mode: gbsp::TAB_*
     int exact = 0;                   // pass-1 twiddles all exact table lookups (no recurrence)
+    int direct = 0;                  // one forward FFT of length cols per row (cols smooth), no Bluestein
+    int* d_drev = nullptr;           // direct: where the forward network leaves each frequency
     int p1_ku = 8, p1_cw = 32;       // pass-1 rows per lane (x32 per item) and window width
     int p1_shape = 1;                // 1-based index of (p1_ku, p1_cw, tab_mode) in the shape table
     int planner = GBSP_PLANNER_MODEL;
@@ -204,6 +206,10 @@ gbsp::P1Args p1_args(const gbsp_plan_s* p, int u0, int n, float2* S, size_t s_pi
     return a;
 }
 
+// The chirp pass 1 multiplies S by: the Bluestein pre-chirp (the channel-0
+// post table, chirp[c] * W^0), or none for direct plans.
+const float2* p1_chirp(const gbsp_plan_s* p) { return p->direct ? nullptr : p->d_post; }
+
 // chirp == nullptr gives the raw column sums (gbsp_column_sums)
 int launch_pass1(const gbsp_plan_s* p, int u0, int n, float2* S, size_t sp, const float2* chirp,
                  cudaStream_t st) {
@@ -234,6 +240,7 @@ gbsp::RowsArgs rows_args(const gbsp_plan_s* p, const float2* S, size_t s_pitch, 
     a.map_lo = map_lo;
     a.map_hi = map_hi;
     a.zscratch = p->d_zscratch;
+    a.drev = p->direct ? p->d_drev : nullptr;
     return a;
 }
 
@@ -340,6 +347,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     p->L = sp.L;
     p->K = sp.K;
     p->Lp = sp.Lp;
+    p->direct = sp.direct;
     p->fd = sp.ranked[0].fd;
     p->rows_threads = sp.ranked[0].nt;
     if (o.stream_tile_rows < GBSP_STREAM_TILE_AUTO)
@@ -435,7 +443,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
                                 (p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW)
                                     ? (size_t)p->rows_grid * (K - 1) * Lp * sizeof(float2)
                                     : 0,
-                                stream_slab, stream_slab};
+                                stream_slab, stream_slab, p->direct ? (size_t)Lp * sizeof(int) : 0};
         size_t total = 0;
         for (size_t b : sizes) total += a256(b);
         void* base = nullptr;
@@ -481,6 +489,7 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
     if ((rc = dev_alloc(p, (void**)&p->d_post, (size_t)K * cols * sizeof(float2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_filt, (size_t)K * Lp * sizeof(float2)))) return rc;
     if ((rc = dev_alloc(p, (void**)&p->d_fftw, (size_t)ntw * sizeof(float2)))) return rc;
+    if (p->direct && (rc = dev_alloc(p, (void**)&p->d_drev, (size_t)Lp * sizeof(int)))) return rc;
     // FP64 filter workspace (ping-pong: the stages run out of place), kept
     // with the plan: freeing it here would synchronise the whole device
     double2* d_spec[2] = {nullptr, nullptr};
@@ -527,17 +536,21 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         gbsp::k_tables<<<blocks_for(n_tab, 256), 256, 0, fs>>>(ta);
     }
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && p->direct) {  // no filter: the digit-reversal table instead
+        gbsp::k_digit_rev<<<blocks_for(Lp, 256), 256, 0, fs>>>(p->d_drev, p->fd);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && !p->direct) {
         gbsp::k_table_filter_input<<<blocks_for((long)K * Lp, 256), 256, 0, fs>>>(d_spec[0], cols, p->L, K, Lp);
         e = cudaGetLastError();
     }
     int cur = 0;
-    for (int s = 0; s < p->fd.nst && e == cudaSuccess; s++, cur ^= 1) {
+    for (int s = 0; s < p->fd.nst && e == cudaSuccess && !p->direct; s++, cur ^= 1) {
         gbsp::k_dif_stage_f64<<<blocks_for((long)K * Lp, 128), 128, 0, fs>>>(d_spec[cur], d_spec[cur ^ 1], K, Lp,
                                                                              p->fd.R[s], p->fd.m[s]);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && !p->direct) {
         gbsp::k_table_filter_final<<<blocks_for((long)K * Lp, 256), 256, 0, fs>>>(
             p->d_filt, d_spec[cur], K, Lp, p->fd.R[p->fd.nst - 1], 1.0 / (double)p->L);
         e = cudaGetLastError();
@@ -666,6 +679,7 @@ int gbsp_plan_get_info(gbsp_plan_t p, gbsp_plan_info* info) {
     info->planner = p->planner;
     info->channel_mode = p->K == 1 ? 0 : (p->row_mode == gbsp::ROW_CLUSTER ? 1 : 2);
     info->exact_phases = p->exact;
+    info->direct = p->direct;
     return GBSP_OK;
 }
 
@@ -689,7 +703,7 @@ int gbsp_execute(gbsp_plan_t p, void* d_out, size_t out_pitch, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     for (int u0 = 0; u0 < p->half_rows; u0 += p->u_tile) {
         const int n = std::min(p->u_tile, p->half_rows - u0);
-        if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p->d_post, st))) return rc;
+        if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p1_chirp(p), st))) return rc;
         if ((rc = launch_rows(p, u0, n, d_out, out_pitch, st))) return rc;
     }
     return GBSP_OK;
@@ -710,7 +724,7 @@ int gbsp_execute_profiled(gbsp_plan_t p, void* d_out, size_t out_pitch, void* st
     for (int t = 0; t < ntiles && rc == GBSP_OK; t++) {
         const int u0 = t * p->u_tile;
         const int n = std::min(p->u_tile, p->half_rows - u0);
-        rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p->d_post, st);
+        rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p1_chirp(p), st);
         if (rc == GBSP_OK && cudaEventRecord(ev[2 * t + 1], st) != cudaSuccess) rc = GBSP_ERR_CUDA;
         if (rc == GBSP_OK) rc = launch_rows(p, u0, n, d_out, out_pitch, st);
         if (rc == GBSP_OK && cudaEventRecord(ev[2 * t + 2], st) != cudaSuccess) rc = GBSP_ERR_CUDA;
@@ -816,7 +830,7 @@ extern "C" int gbsp_execute_noalloc(gbsp_plan_t p, void* d_out, size_t out_pitch
     cudaStream_t st = (cudaStream_t)stream;
     for (int u0 = 0; u0 < p->half_rows; u0 += tile) {
         const int n = std::min(tile, p->half_rows - u0);
-        if ((rc = launch_pass1(p, u0, n, (float2*)scratch, p->s_pitch, p->d_post, st))) return rc;
+        if ((rc = launch_pass1(p, u0, n, (float2*)scratch, p->s_pitch, p1_chirp(p), st))) return rc;
         if ((rc = launch_rows_from(p, (const float2*)scratch, p->s_pitch, u0, n, d_out, out_pitch, st)))
             return rc;
     }
@@ -1049,7 +1063,7 @@ int gbsp_batch_create(int count, const gbsp_matrix* mats, const gbsp_options* op
         const int ublk = 32 * b->ku;
         for (int k = 0; k < n; k++) {
             const gbsp_plan_s* p = b->plans[b->order[k]];
-            p1[k] = p1_args(p, 0, p->half_rows, p->d_S, p->s_pitch, p->d_post);
+            p1[k] = p1_args(p, 0, p->half_rows, p->d_S, p->s_pitch, p1_chirp(p));
             p1b[k + 1] = p1b[k] + (long)((p->half_rows + ublk - 1) / ublk) * ((p->s_cols + p->p1_cw - 1) / p->p1_cw);
         }
         for (const auto& c : b->classes) {
@@ -1229,7 +1243,7 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
         if (2 * u_last == p->rows) hi_first++;  // the middle row is its own mirror
         const int hi_last = p->rows - std::max(u0, 1);
         const int n_hi = std::max(0, hi_last - hi_first + 1);
-        if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p->d_post, st))) break;
+        if ((rc = launch_pass1(p, u0, n, p->d_S, p->s_pitch, p1_chirp(p), st))) break;
         // only the row kernel writes the slab: pass 1 overlaps the copy
         // that still drains it
         if (t >= 2) GB_CUDA(cudaStreamWaitEvent(st, r.copied[b], 0));

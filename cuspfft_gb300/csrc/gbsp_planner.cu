@@ -50,7 +50,7 @@ int build_fft_desc(int Lp, const std::vector<int>& rs, FFTDesc* fd) {
 int fft_tw_count(const FFTDesc& fd) { return fd.rest_base + fd.rest_len; }
 
 size_t rows_smem_bytes(const FFTDesc& fd) {
-    return ((size_t)fd.Lp + (size_t)fd.rest_len) * sizeof(float2);
+    return ((size_t)row_buf_len(fd.Lp) + (size_t)fd.rest_len) * sizeof(float2);
 }
 
 // ---- radix planning -------------------------------------------------------
@@ -158,10 +158,25 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
     const int nt_opt = o ? o->rows_threads : 0;
     if (nt_opt < 0 || nt_opt % 32 || nt_opt > 1024)
         return set_error(GBSP_ERR_INVALID, "rows_threads must be 0 or a multiple of 32 up to 1024");
+    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 24000;
+    // Direct: when cols itself has the policy's smoothness and fits one CTA,
+    // the row DFT is one forward FFT of length cols -- the same DFT as the
+    // Bluestein convolution, with a quarter of its FFT work and less rounding
+    out->direct = 0;
+    if (!(o && o->force_bluestein) && cols >= 2 && cols <= maxLp && next_smooth(cols, policy) == cols) {
+        auto ranked = rank_radices(cols, smem_cap, o ? o->radix : nullptr, nt_opt);
+        if (!ranked.empty()) {
+            out->L = cols;
+            out->K = 1;
+            out->Lp = cols;
+            out->direct = 1;
+            out->ranked = std::move(ranked);
+            return GBSP_OK;
+        }
+    }
     long L = next_smooth(2L * cols - 1, policy);
     if (L < 2) L = 2;
     if (L > (1L << 28)) return set_error(GBSP_ERR_UNSUPPORTED, "fft_len too large");
-    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 24000;
     out->L = (int)L;
     out->K = 0;
     // more than MAX_CHANNELS channels only run sequentially in one CTA

@@ -32,6 +32,7 @@ std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_op
 // whose channel length fits; ranked radix choices for that channel.
 struct ChannelSplit {
     int L = 0, K = 0, Lp = 0;
+    int direct = 0;  // 1: one forward FFT of length cols (cols smooth), no Bluestein
     std::vector<RadixPlan> ranked;
 };
 int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSplit* out);

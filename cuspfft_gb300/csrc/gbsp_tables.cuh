@@ -146,6 +146,20 @@ __device__ __forceinline__ float2 chirp_twiddle(long long c, int q, int cols, in
     return make_float2((float)co, (float)s);
 }
 
+// Direct plans: drev[f] = position of frequency f after the forward DIF
+// network, sum over stages s of digit_s(f) * m_s, where digit_s(f) =
+// (f / (R_0 ... R_{s-1})) mod R_s (the stage-s output q lands at q * m_s).
+__global__ void k_digit_rev(int* drev, FFTDesc fd) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= fd.Lp) return;
+    int t = f, pos = 0;
+    for (int s = 0; s < fd.nst; s++) {
+        pos += (t % fd.R[s]) * fd.m[s];
+        t /= fd.R[s];
+    }
+    drev[f] = pos;
+}
+
 // exp(-2*pi*i*e/n) for an exactly reduced integer phase e < n
 __device__ __forceinline__ float2 root_f32(long long e, long long n) {
     double s, c;

@@ -150,7 +150,8 @@ class Plan:
     def __init__(self, coo: COOMatrix, *, length_policy: int = 0, u_tile: int = 0,
                  kahan_min_degree: int = 0, index_bytes: int = 0, max_channel_len: int = 0,
                  rows_threads: int = 0, row_table_mode: int = 0, radix=None, pass1_shape: int = 0,
-                 channel_mode: int = 0, stream_tile_rows: int = 0, exact_phases: int = 0, planner=None,
+                 channel_mode: int = 0, stream_tile_rows: int = 0, exact_phases: int = 0,
+                 force_bluestein: int = 0, planner=None,
                  options: Optional[GbspOptions] = None, stream=None,
                  csc: Optional[CompactCSC] = None):
         lib = load()
@@ -162,7 +163,8 @@ class Plan:
                          kahan_min_degree=kahan_min_degree, index_bytes=index_bytes,
                          max_channel_len=max_channel_len, rows_threads=rows_threads,
                          row_table_mode=row_table_mode, pass1_shape=pass1_shape, channel_mode=channel_mode,
-                         stream_tile_rows=stream_tile_rows, exact_phases=exact_phases)
+                         stream_tile_rows=stream_tile_rows, exact_phases=exact_phases,
+                         force_bluestein=force_bluestein)
         cp = np.ascontiguousarray(csc.col_ptr, np.int32)
         ri = np.ascontiguousarray(csc.row_idx if coo.nnz else np.zeros(1, np.int32), np.int32)
         sc = np.ascontiguousarray(csc.sparse_cols if csc.n_sparse_cols else np.zeros(1, np.int32),

@@ -109,6 +109,11 @@ typedef struct {
                               three-term-recurrence steps (two FMAs) between; 1 = the table
                               entry at the exact phase for every row (no float products
                               beyond the table's rounding; slower)                        */
+    int force_bluestein;   /* 0 = default: when cols itself is smooth for the length
+                              policy (3-smooth, 7-smooth or a power of two) and fits one
+                              CTA, each row is one forward FFT of length cols (the same
+                              DFT, a quarter of the work, fft_len = cols); 1 = always the
+                              Bluestein convolution, as the reference computes it        */
 } gbsp_options;
 
 typedef struct {
@@ -131,6 +136,7 @@ typedef struct {
     int planner;           /* planner that chose the configuration                        */
     int channel_mode;      /* 0 single channel, 1 clusters, 2 sequential channels         */
     int exact_phases;      /* 1: every pass-1 twiddle an exact table lookup               */
+    int direct;            /* 1: one FFT of length cols per row instead of Bluestein       */
 } gbsp_plan_info;
 
 int         gbsp_version(void);

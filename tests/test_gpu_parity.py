@@ -382,3 +382,25 @@ def test_every_pass1_shape(cuda, shape):
     got, info = run_plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, pass1_shape=shape)
     assert info["pass1_shape"] == shape
     check_against_oracle(coo, got)
+
+
+@pytest.mark.parametrize("policy,cols", [(gb.GBSP_LEN_7SMOOTH, 2048), (gb.GBSP_LEN_7SMOOTH, 1029),
+                                         (gb.GBSP_LEN_7SMOOTH, 375), (gb.GBSP_LEN_3SMOOTH, 243),
+                                         (gb.GBSP_LEN_3SMOOTH, 1536), (gb.GBSP_LEN_POW2, 256),
+                                         (gb.GBSP_LEN_7SMOOTH, 2), (gb.GBSP_LEN_7SMOOTH, 7)])
+def test_direct_row_fft(cuda, policy, cols):
+    # cols already smooth for the policy: each row is one forward FFT of
+    # length cols (fft_len = cols), the same DFT as the Bluestein convolution
+    # that force_bluestein restores; odd lengths included (the row buffer is
+    # padded to even for the bulk copy)
+    g = np.random.default_rng(cols)
+    rows = 301
+    n = max(1, rows * cols // 20)
+    coo = synthetic.normalise(rows, cols, g.integers(0, rows, n), g.integers(0, cols, n))
+    got, info = run_plan(coo, length_policy=policy)
+    assert info["direct"] == 1 and info["fft_len"] == cols and info["channels"] == 1
+    check_against_oracle(coo, got)
+    blu, binfo = run_plan(coo, length_policy=policy, force_bluestein=1)
+    assert binfo["direct"] == 0 and binfo["fft_len"] >= 2 * cols - 1
+    check_against_oracle(coo, blu)
+    assert fp64.rel_l2(got, blu) < 1e-5

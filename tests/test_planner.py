@@ -3,10 +3,12 @@
 For every shape and length policy, each candidate the planner offers
 (gbsp_plan_candidates) must describe a transform the kernels can run: radices
 the row kernel is compiled for, a channel length (their product) that divides
-the Bluestein length of the policy -- next 3-smooth, 7-smooth or power of two
->= 2*cols - 1, as the reference computes it (oracle/ref_port.py, pinned to the
-reference's own functions) -- into at most 64 channels, a whole number of
-warps per block and a pass-1 shape index in range.
+the row's FFT length into at most 64 channels, a whole number of warps per
+block and a pass-1 shape index in range.  The FFT length is the Bluestein
+length of the policy -- next 3-smooth, 7-smooth or power of two >= 2*cols - 1,
+as the reference computes it (oracle/ref_port.py, pinned to the reference's
+own functions) -- or, when cols itself has the policy's smoothness and fits
+one CTA, cols (one direct FFT per row; force_bluestein restores the former).
 """
 import numpy as np
 import pytest
@@ -26,6 +28,15 @@ def bluestein_length(cols: int, policy: int) -> int:
     return ref_port.next_smooth(n, seven=policy == gb.GBSP_LEN_7SMOOTH)
 
 
+def row_fft_length(cols: int, policy: int, force_bluestein: bool = False) -> int:
+    if not force_bluestein and 2 <= cols <= 24000:
+        smooth = ref_port.next_power_of_two(cols) if policy == gb.GBSP_LEN_POW2 else \
+            ref_port.next_smooth(cols, seven=policy == gb.GBSP_LEN_7SMOOTH)
+        if smooth == cols:
+            return cols
+    return bluestein_length(cols, policy)
+
+
 SHAPES = [(5, 8), (64, 97), (1000, 999), (3001, 2048), (8219, 8219), (16706, 16706), (40421, 40421),
           (131071, 33), (33, 120001), (5, 200003)]
 
@@ -33,8 +44,8 @@ SHAPES = [(5, 8), (64, 97), (1000, 999), (3001, 2048), (8219, 8219), (16706, 167
 @pytest.mark.parametrize("policy", [gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH, gb.GBSP_LEN_POW2])
 @pytest.mark.parametrize("rows,cols", SHAPES)
 def test_candidates_are_runnable(rows, cols, policy):
-    L = bluestein_length(cols, policy)
-    assert gb.next_smooth(2 * cols - 1, policy) == L
+    assert gb.next_smooth(2 * cols - 1, policy) == bluestein_length(cols, policy)
+    L = row_fft_length(cols, policy)
     cands, nr, npp = tuning.candidates(rows, cols, length_policy=policy)
     assert nr >= 1 and npp >= 1 and len(cands) == nr * npp
     for c in cands:
@@ -53,4 +64,6 @@ def test_single_channel_when_the_row_fits(rows, cols):
     # a row that fits one CTA's shared memory runs as one channel
     for policy in (gb.GBSP_LEN_3SMOOTH, gb.GBSP_LEN_7SMOOTH):
         cands, _, _ = tuning.candidates(rows, cols, length_policy=policy)
-        assert all(int(np.prod(c.radices())) == bluestein_length(cols, policy) for c in cands)
+        assert all(int(np.prod(c.radices())) == row_fft_length(cols, policy) for c in cands)
+        forced, _, _ = tuning.candidates(rows, cols, length_policy=policy, force_bluestein=1)
+        assert all(int(np.prod(c.radices())) == bluestein_length(cols, policy) for c in forced)
