@@ -497,7 +497,10 @@ struct RowsArgs {
 //               results wait in an L2-resident scratch for the combine
 //   ROW_SEQW    ROW_SEQ for more than MAX_CHANNELS channels (very wide rows;
 //               a separate instance, so the common one keeps its registers)
-constexpr int ROW_SINGLE = 0, ROW_CLUSTER = 1, ROW_SEQ = 2, ROW_SEQW = 3;
+//   ROW_DIRECT  K == 1 and a direct plan (cols smooth: one forward FFT of
+//               length cols, no Bluestein convolution), its own instance so
+//               the Bluestein one keeps its registers
+constexpr int ROW_SINGLE = 0, ROW_CLUSTER = 1, ROW_SEQ = 2, ROW_SEQW = 3, ROW_DIRECT = 4;
 
 // One Bluestein row t of the tile (u = u0 + t), channel q of K: input,
 // forward network, filter, inverse network, Hermitian-paired output.  Whole
@@ -505,12 +508,14 @@ constexpr int ROW_SINGLE = 0, ROW_CLUSTER = 1, ROW_SEQ = 2, ROW_SEQW = 3;
 // overwrite buf at once.  Direct plans (a.drev set, K = 1) run only the
 // forward network over the row's cols points and gather the spectrum through
 // drev in the writer.
-template <int MAXR, int MODE>
+// DIRECT: 0 never (Bluestein), 1 always (ROW_DIRECT), 2 per row from a.drev
+// (the batched kernel, whose matrices mix both kinds)
+template <int MAXR, int MODE, int DIRECT = (MODE == ROW_DIRECT ? 1 : 0)>
 __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& fd, int t, int q, float2* buf,
                                               const float2* twr, const float2* const* zsrc, uint64_t* bar,
                                               uint32_t& parity, int& err_bits) {
     constexpr bool CLUSTER = MODE == ROW_CLUSTER;
-    constexpr bool MULTI = MODE != ROW_SINGLE;
+    constexpr bool MULTI = MODE == ROW_CLUSTER || MODE == ROW_SEQ || MODE == ROW_SEQW;
     constexpr bool SEQ = MODE == ROW_SEQ || MODE == ROW_SEQW;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int Lp = fd.Lp, K = a.K, cols = a.cols;
@@ -523,7 +528,7 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     auto tw_smem = [&](int s) -> const float2* { return twr + (fd.twoff[s] - fd.rest_base); };
     const int u = a.u0 + t;
     const float2* srow = a.S + (size_t)t * a.s_pitch;
-    const bool direct = !MULTI && a.drev != nullptr;
+    const bool direct = DIRECT == 1 || (DIRECT == 2 && a.drev != nullptr);
     bool ok = true;
     // ROW_SEQ runs every channel of the row here; the other modes one
     const int q_end = SEQ ? K : q + 1;
@@ -768,15 +773,18 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     else __syncthreads();
 }
 
-// MODE: ROW_SINGLE, ROW_CLUSTER (launched with a K-CTA cluster dimension)
-// or ROW_SEQ; single-channel plans use the ROW_SINGLE instance, which
-// carries no multi-channel code.
+// MODE: ROW_SINGLE, ROW_DIRECT, ROW_CLUSTER (launched with a K-CTA cluster
+// dimension), ROW_SEQ or ROW_SEQW; single-channel plans use the ROW_SINGLE
+// (or ROW_DIRECT) instance, which carries no multi-channel code.
 template <int NTMAX, int MODE>
 __global__ void __launch_bounds__(NTMAX, 1) k_bluestein_rows(RowsArgs a, FFTDesc fd, int* err) {
     extern __shared__ float4 smem_raw[];
     __shared__ uint64_t in_bar;
     float2* buf = reinterpret_cast<float2*>(smem_raw);
-    float2* twr = buf + row_buf_len(fd.Lp);
+    // only a direct row can have odd Lp = cols below its even bulk-copy length
+    // (a Bluestein row has Lp >= 2 cols - 1 and the multi-channel loads skip
+    // the bulk copy when the row does not fit)
+    float2* twr = buf + (MODE == ROW_DIRECT ? row_buf_len(fd.Lp) : fd.Lp);
     for (int i = threadIdx.x; i < fd.rest_len; i += blockDim.x) twr[i] = a.fft_tw[fd.rest_base + i];
     if (threadIdx.x == 0) mbar_init(&in_bar, 1);
 
@@ -865,7 +873,7 @@ k_bluestein_rows_batch(const RowsBatch* __restrict__ descs, const long* __restri
             __syncthreads();
             loaded = m;
         }
-        bluestein_row<MAXR, ROW_SINGLE>(cur.a, cur.fd, (int)(t - row_begin[m]), 0, buf, twr, zsrc, &in_bar, parity,
+        bluestein_row<MAXR, ROW_SINGLE, 2>(cur.a, cur.fd, (int)(t - row_begin[m]), 0, buf, twr, zsrc, &in_bar, parity,
                             err_bits);
     }
     if (err_bits) atomicOr(err, err_bits);

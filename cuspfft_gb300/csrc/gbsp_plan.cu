@@ -61,7 +61,7 @@ struct gbsp_plan_s {
     int p1_grid = 0;
     size_t p1_smem = 0;
     int rows_grid = 0, rows_threads = 1024, rows_ntmax = 1024;
-    int row_mode = 0;                // gbsp::ROW_SINGLE / ROW_CLUSTER / ROW_SEQ
+    int row_mode = 0;                // gbsp::ROW_SINGLE / ROW_DIRECT / ROW_CLUSTER / ROW_SEQ / ROW_SEQW
     float2* d_zscratch = nullptr;    // ROW_SEQ: rows_grid x (K-1) x Lp channel results
     size_t rows_smem = 0;
     size_t device_bytes = 0;
@@ -264,7 +264,7 @@ int rows_prepare(gbsp_plan_s* p, int sms) {
         return set_error(GBSP_ERR_INVALID, "rows_threads must be a multiple of 32, at most 512 when a "
                                            "radix exceeds 16, at most 1024 otherwise");
     using namespace gbsp;
-    if (p->K == 1) p->row_mode = ROW_SINGLE;
+    if (p->K == 1) p->row_mode = p->direct ? ROW_DIRECT : ROW_SINGLE;
     else if (p->row_mode != ROW_SEQ || p->rows_ntmax != 512) p->row_mode = ROW_CLUSTER;
     if (p->row_mode == ROW_CLUSTER && p->K > MAX_CHANNELS)
         return set_error(GBSP_ERR_UNSUPPORTED, "more than " + std::to_string(MAX_CHANNELS) +

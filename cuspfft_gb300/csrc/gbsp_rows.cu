@@ -1,14 +1,14 @@
-// gbsp_rows.cu -- the single-channel Bluestein row kernel (both block-size
-// bounds), the batched row kernel, and the host launch functions; the
+// gbsp_rows.cu -- the single-channel row kernels, Bluestein and direct (both
+// block-size bounds), the batched row kernel, and the host launch functions; the
 // multi-channel modes compile in gbsp_rows_multi.cu.
 #include "gbsp_launch.h"
 
 namespace gbsp {
 namespace {
 
-template <int NTMAX>
+template <int NTMAX, int MODE>
 int single_capacity(const RowsKernel& k, int sms, int* cap) {
-    auto kern = k_bluestein_rows<NTMAX, ROW_SINGLE>;
+    auto kern = k_bluestein_rows<NTMAX, MODE>;
     if (int rc = allow_full_smem((const void*)kern)) return rc;
     int nb = 0;
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, k.nt, k.smem));
@@ -16,9 +16,9 @@ int single_capacity(const RowsKernel& k, int sms, int* cap) {
     return GBSP_OK;
 }
 
-template <int NTMAX>
+template <int NTMAX, int MODE>
 int single_launch(const RowsKernel& k, int grid, cudaStream_t st, const RowsArgs& a, const FFTDesc& fd, int* err) {
-    k_bluestein_rows<NTMAX, ROW_SINGLE><<<grid, k.nt, k.smem, st>>>(a, fd, err);
+    k_bluestein_rows<NTMAX, MODE><<<grid, k.nt, k.smem, st>>>(a, fd, err);
     GB_CUDA(cudaGetLastError());
     return GBSP_OK;
 }
@@ -27,13 +27,21 @@ int single_launch(const RowsKernel& k, int grid, cudaStream_t st, const RowsArgs
 
 int rows_capacity(const RowsKernel& k, int sms, int* cap) {
     *cap = 0;
+    if (k.mode == ROW_DIRECT)
+        return k.ntmax == 512 ? single_capacity<512, ROW_DIRECT>(k, sms, cap)
+                              : single_capacity<1024, ROW_DIRECT>(k, sms, cap);
     if (k.mode != ROW_SINGLE) return rows_capacity_multi(k, sms, cap);
-    return k.ntmax == 512 ? single_capacity<512>(k, sms, cap) : single_capacity<1024>(k, sms, cap);
+    return k.ntmax == 512 ? single_capacity<512, ROW_SINGLE>(k, sms, cap)
+                          : single_capacity<1024, ROW_SINGLE>(k, sms, cap);
 }
 
 int rows_launch(const RowsKernel& k, int grid, cudaStream_t st, const RowsArgs& a, const FFTDesc& fd, int* err) {
+    if (k.mode == ROW_DIRECT)
+        return k.ntmax == 512 ? single_launch<512, ROW_DIRECT>(k, grid, st, a, fd, err)
+                              : single_launch<1024, ROW_DIRECT>(k, grid, st, a, fd, err);
     if (k.mode != ROW_SINGLE) return rows_launch_multi(k, grid, st, a, fd, err);
-    return k.ntmax == 512 ? single_launch<512>(k, grid, st, a, fd, err) : single_launch<1024>(k, grid, st, a, fd, err);
+    return k.ntmax == 512 ? single_launch<512, ROW_SINGLE>(k, grid, st, a, fd, err)
+                          : single_launch<1024, ROW_SINGLE>(k, grid, st, a, fd, err);
 }
 
 int rows_batch_blocks_per_sm(int nt, size_t smem, int* nb) {
