@@ -158,12 +158,20 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
     const int nt_opt = o ? o->rows_threads : 0;
     if (nt_opt < 0 || nt_opt % 32 || nt_opt > 1024)
         return set_error(GBSP_ERR_INVALID, "rows_threads must be 0 or a multiple of 32 up to 1024");
-    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 24000;
+    // By default a channel is as long as shared memory allows (the row
+    // buffer plus the inner stages' twiddles, about 28k points on GB300):
+    // fewer channels were faster at every length measured (a cap of 24000
+    // had split cols 25000 into four channels, 1.88 ms against 0.37 ms for
+    // the direct FFT in one; 40421^2 into five, 32.6 against 30.5 ms for three)
+    const int maxLp = (o && o->max_channel_len > 0) ? o->max_channel_len : 0;
+    auto channel_fits = [&](long lp) {
+        return lp >= 2 && (maxLp == 0 || lp <= maxLp) && (size_t)row_buf_len((int)lp) * sizeof(float2) <= smem_cap;
+    };
     // Direct: when cols itself has the policy's smoothness and fits one CTA,
     // the row DFT is one forward FFT of length cols -- the same DFT as the
     // Bluestein convolution, with a quarter of its FFT work and less rounding
     out->direct = 0;
-    if (!(o && o->force_bluestein) && cols >= 2 && cols <= maxLp && next_smooth(cols, policy) == cols) {
+    if (!(o && o->force_bluestein) && channel_fits(cols) && next_smooth(cols, policy) == cols) {
         auto ranked = rank_radices(cols, smem_cap, o ? o->radix : nullptr, nt_opt);
         if (!ranked.empty()) {
             out->L = cols;
@@ -182,7 +190,7 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
     // more than MAX_CHANNELS channels only run sequentially in one CTA
     const int kmax = (o && o->channel_mode == 1) ? MAX_CHANNELS : MAX_SEQ_CHANNELS;
     for (int k = 1; k <= kmax; k++) {
-        if (L % k || L / k > maxLp || L / k < 2) continue;
+        if (L % k || !channel_fits(L / k)) continue;
         auto ranked = rank_radices((int)(L / k), smem_cap, o ? o->radix : nullptr, nt_opt);
         if (ranked.empty()) continue;
         out->K = k;
@@ -191,8 +199,9 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
         return GBSP_OK;
     }
     return set_error(GBSP_ERR_UNSUPPORTED, "fft_len " + std::to_string(L) + " does not split into <= " +
-                                               std::to_string(kmax) + " channels of <= " +
-                                               std::to_string(maxLp) + " that fit in shared memory");
+                                               std::to_string(kmax) + " channels" +
+                                               (maxLp > 0 ? " of <= " + std::to_string(maxLp) : std::string()) +
+                                               " that fit in shared memory");
 }
 
 // Shapes by index (the 1-based gbsp_options.pass1_shape minus one).  Window

@@ -84,8 +84,9 @@ typedef struct {
                               compensation; 0 = default 64; negative = never (plain FP32) */
     int index_bytes;       /* 0 = auto (2 when rows,cols <= 65536, else 4), or 2 / 4      */
     int max_channel_len;   /* largest per-CTA FFT length held in shared memory;
-                              0 = default; longer convolutions split into channels that
-                              run as one thread-block cluster                             */
+                              0 = as long as shared memory allows (about 28k points);
+                              longer convolutions split into channels (a thread-block
+                              cluster, or one CTA running them in turn)                   */
     int rows_threads;      /* row-kernel block size: 0 = auto, else a multiple of 32
                               in [64, 1024] (at most 512 when a radix exceeds 16)         */
     int row_table_mode;    /* pass-1 twiddle table: 0 = auto, 1 = full circle,

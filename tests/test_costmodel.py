@@ -31,7 +31,7 @@ def test_candidates_large_rows_prefer_two_level_table():
     # half table), the half-table and two-level 128-row shapes follow
     cands, nr, npp = tuning.candidates(40421, 40421, length_policy=gb.GBSP_LEN_7SMOOTH)
     assert npp == 3 and [c.pass1_shape for c in cands[:3]] == [7, 6, 8]
-    assert all(int(np.prod(c.radices())) * 5 == 81000 for c in cands)
+    assert all(int(np.prod(c.radices())) * 3 == 81000 for c in cands)  # three channels of 27000
 
 
 def test_features_are_separable():

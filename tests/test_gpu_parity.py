@@ -284,7 +284,8 @@ def test_two_level_table_on_request(cuda):
 
 @pytest.mark.parametrize("rows,cols", [(33, 120001), (5, 200003)])
 def test_wide_matrices_many_channels(cuda, rows, cols):
-    # the convolution needs more channels than a cluster holds (L > 8 x 24000):
+    # the convolution needs more channels than a cluster holds (L = 240100 and
+    # 401408, channels of at most ~28k points):
     # one CTA runs them in turn
     g = np.random.default_rng(cols)
     n = 4 * cols
@@ -296,8 +297,11 @@ def test_wide_matrices_many_channels(cuda, rows, cols):
         gb.Plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, channel_mode=1)
 
 
-@pytest.mark.parametrize("policy,channels", [(gb.GBSP_LEN_3SMOOTH, 4), (gb.GBSP_LEN_7SMOOTH, 5)])
-def test_config_40421_uint32_indices(cuda, policy, channels):
+# L = 82944 (3-smooth) and 81000 (7-smooth) run as three channels of 27648 and
+# 27000 points; a 24000-point cap keeps the five-channel form covered
+@pytest.mark.parametrize("policy,max_len,channels", [(gb.GBSP_LEN_3SMOOTH, 0, 3), (gb.GBSP_LEN_7SMOOTH, 0, 3),
+                                                     (gb.GBSP_LEN_7SMOOTH, 24000, 5)])
+def test_config_40421_uint32_indices(cuda, policy, max_len, channels):
     # the largest configuration: 40421^2 power-law adjacency, ~351k nnz,
     # 4-byte row indices (the reference's int32 pass 1,
     # src/sparse_fft_bluestein.cu:334-364), 6.5 GB output; the convolution
@@ -309,7 +313,7 @@ def test_config_40421_uint32_indices(cuda, policy, channels):
     us = np.unique(np.concatenate([[0, 1, 2, coo.rows // 2, coo.rows // 2 + 1, coo.rows - 1],
                                    g.integers(0, coo.rows, 14)]))
     fc = coo.cols // 2 + 1
-    with gb.Plan(coo, length_policy=policy, index_bytes=4) as plan:
+    with gb.Plan(coo, length_policy=policy, index_bytes=4, max_channel_len=max_len) as plan:
         info = plan.info
         assert info["index_bytes"] == 4
         assert info["channels"] == channels and info["channel_mode"] == 2
@@ -387,7 +391,9 @@ def test_every_pass1_shape(cuda, shape):
 @pytest.mark.parametrize("policy,cols", [(gb.GBSP_LEN_7SMOOTH, 2048), (gb.GBSP_LEN_7SMOOTH, 1029),
                                          (gb.GBSP_LEN_7SMOOTH, 375), (gb.GBSP_LEN_3SMOOTH, 243),
                                          (gb.GBSP_LEN_3SMOOTH, 1536), (gb.GBSP_LEN_POW2, 256),
-                                         (gb.GBSP_LEN_7SMOOTH, 2), (gb.GBSP_LEN_7SMOOTH, 7)])
+                                         (gb.GBSP_LEN_7SMOOTH, 2), (gb.GBSP_LEN_7SMOOTH, 7),
+                                         (gb.GBSP_LEN_7SMOOTH, 25000), (gb.GBSP_LEN_7SMOOTH, 25725),
+                                         (gb.GBSP_LEN_3SMOOTH, 26244)])
 def test_direct_row_fft(cuda, policy, cols):
     # cols already smooth for the policy: each row is one forward FFT of
     # length cols (fft_len = cols), the same DFT as the Bluestein convolution
@@ -395,7 +401,7 @@ def test_direct_row_fft(cuda, policy, cols):
     # padded to even for the bulk copy)
     g = np.random.default_rng(cols)
     rows = 301
-    n = max(1, rows * cols // 20)
+    n = min(max(1, rows * cols // 20), 60000)
     coo = synthetic.normalise(rows, cols, g.integers(0, rows, n), g.integers(0, cols, n))
     got, info = run_plan(coo, length_policy=policy)
     assert info["direct"] == 1 and info["fft_len"] == cols and info["channels"] == 1

@@ -29,7 +29,9 @@ def bluestein_length(cols: int, policy: int) -> int:
 
 
 def row_fft_length(cols: int, policy: int, force_bluestein: bool = False) -> int:
-    if not force_bluestein and 2 <= cols <= 24000:
+    # a smooth row runs as one FFT of length cols when its buffer fits in
+    # shared memory (227 KB on GB300)
+    if not force_bluestein and 2 <= cols and cols * 8 <= 227 * 1024:
         smooth = ref_port.next_power_of_two(cols) if policy == gb.GBSP_LEN_POW2 else \
             ref_port.next_smooth(cols, seven=policy == gb.GBSP_LEN_7SMOOTH)
         if smooth == cols:
