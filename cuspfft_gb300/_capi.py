@@ -38,7 +38,7 @@ EXPORTED = (
     "gbsp_plan_error_flags", "gbsp_device_flags_status", "gbsp_execute_noalloc", "gbsp_batch_create", "gbsp_batch_set_outputs",
     "gbsp_batch_execute", "gbsp_batch_graph_launch", "gbsp_batch_plan_info", "gbsp_batch_error_flags",
     "gbsp_batch_destroy", "gbsp_plan_candidates", "gbsp_plan_features", "gbsp_autotune", "gbsp_mlp_param_count",
-    "gbsp_mlp_forward", "gbsp_mlp_work_floats", "gbsp_mlp_backward", "gbsp_mlp_adam", "gbsp_cost_model_set",
+    "gbsp_mlp_forward", "gbsp_mlp_work_floats", "gbsp_mlp_backward", "gbsp_mlp_adam", "gbsp_cost_model_set", "gbsp_cost_model_set_domain",
     "gbsp_execute_to_host", "gbsp_set_memory_cache",
 )
 
@@ -157,6 +157,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbsp_mlp_backward.argtypes = [vp, i32, vp, vp, i32, vp, vp, vp, vp]
     lib.gbsp_mlp_adam.argtypes = [vp, vp, vp, vp, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp]
     lib.gbsp_cost_model_set.argtypes = [fp, i32, fp, fp]
+    lib.gbsp_cost_model_set_domain.argtypes = [i32, fp, fp]
     lib.gbsp_execute_to_host.argtypes = [vp, vp, C.c_size_t, i32, vp]
     for name in EXPORTED:
         if name not in ("gbsp_status_string", "gbsp_free", "gbsp_mlp_param_count", "gbsp_mlp_work_floats"):

@@ -205,7 +205,8 @@ def train(ds: dict, train_idx, *, epochs: int = 300, batch: int = 1024, lr: floa
         hist.append(tot / n)
         if log_every and (ep + 1) % log_every == 0:
             print(f"train: epoch {ep + 1}/{epochs} mse(log ms) {hist[-1]:.5f}", flush=True)
-    return {"params": net.params(), "mean": mean, "scale": scale, "loss_history": np.asarray(hist, np.float32)}
+    return {"params": net.params(), "mean": mean, "scale": scale, "loss_history": np.asarray(hist, np.float32),
+            "lo": X.min(0), "hi": X.max(0)}
 
 
 def predict(model: dict, X: np.ndarray) -> np.ndarray:
@@ -216,15 +217,33 @@ def predict(model: dict, X: np.ndarray) -> np.ndarray:
     return net.forward(Xs).cpu().numpy()
 
 
+# the library's rule (gbsp_cost_model_set_domain): a feature may leave the
+# training range by at most this fraction of the range's width
+DOMAIN_MARGIN = 0.1
+
+
+def in_domain(model: dict, X: np.ndarray) -> bool:
+    """True when every candidate's features lie in the model's training
+    range (with the library's margin); always true without a range."""
+    if "lo" not in model:
+        return True
+    m = DOMAIN_MARGIN * (model["hi"] - model["lo"])
+    return bool(np.all((X >= model["lo"] - m) & (X <= model["hi"] + m)))
+
+
 def save_model(path, model: dict, meta: dict) -> None:
+    extra = {k: model[k] for k in ("lo", "hi") if k in model}
     np.savez(path, params=model["params"], mean=model["mean"], scale=model["scale"],
-             loss_history=model.get("loss_history", np.zeros(0, np.float32)), meta=json.dumps(meta))
+             loss_history=model.get("loss_history", np.zeros(0, np.float32)), meta=json.dumps(meta), **extra)
 
 
 def load_model(path=DEFAULT_MODEL) -> dict:
     z = np.load(path, allow_pickle=False)
-    return {"params": z["params"].astype(np.float32), "mean": z["mean"].astype(np.float32),
-            "scale": z["scale"].astype(np.float32), "meta": json.loads(str(z["meta"]))}
+    m = {"params": z["params"].astype(np.float32), "mean": z["mean"].astype(np.float32),
+         "scale": z["scale"].astype(np.float32), "meta": json.loads(str(z["meta"]))}
+    if "lo" in z.files:  # training range of every feature (the planner's domain)
+        m["lo"], m["hi"] = z["lo"].astype(np.float32), z["hi"].astype(np.float32)
+    return m
 
 
 def install(model: dict) -> None:
@@ -236,6 +255,11 @@ def install(model: dict) -> None:
     s = np.ascontiguousarray(model["scale"], np.float32)
     check(lib.gbsp_cost_model_set(p.ctypes.data_as(fp), GBSP_N_FEATURES, m.ctypes.data_as(fp),
                                   s.ctypes.data_as(fp)), "gbsp_cost_model_set")
+    if "lo" in model:
+        lo = np.ascontiguousarray(model["lo"], np.float32)
+        hi = np.ascontiguousarray(model["hi"], np.float32)
+        check(lib.gbsp_cost_model_set_domain(GBSP_N_FEATURES, lo.ctypes.data_as(fp), hi.ctypes.data_as(fp)),
+              "gbsp_cost_model_set_domain")
 
 
 _installed = False
@@ -300,17 +324,23 @@ def main(argv=None) -> None:
 
 def evaluate_large(model: dict) -> dict:
     """The 40421 x 40421 power-law adjacency (~351k nnz, 4-byte indices):
-    exhaustive tuning against the learned and the analytic choice."""
+    exhaustive tuning against the learned planner's choice (the network's
+    pick inside its training range, else the analytic one), the network's
+    own pick and the analytic choice."""
     coo = synthetic.config_matrix("uniform_powerlaw_40421")
     ds = collect([coo], reps=2, log_every=0, index_bytes=4)
     X, _, _ = compose(ds, [0])
     pred = predict(model, X)
     nr, npp = int(ds["n_rows"][0]), int(ds["n_p1"][0])
     t = ds["ms_rows"][0, :nr, None].astype(np.float64) + ds["ms_pass1"][0, None, :npp]
+    net_ms = float(t.ravel()[int(np.argmin(pred))])
+    inside = in_domain(model, X)
+    learned_ms = net_ms if inside else float(t[0, 0])
     return {"shape": [coo.rows, coo.cols], "nnz": coo.nnz, "index_bytes": 4, "candidates": nr * npp,
-            "best_ms": float(t.min()), "learned_ms": float(t.ravel()[int(np.argmin(pred))]),
-            "analytic_ms": float(t[0, 0]),
-            "regret_learned": float(t.ravel()[int(np.argmin(pred))] / t.min() - 1.0),
+            "in_domain": inside, "best_ms": float(t.min()), "learned_ms": learned_ms,
+            "network_ms": net_ms, "analytic_ms": float(t[0, 0]),
+            "regret_learned": learned_ms / float(t.min()) - 1.0,
+            "regret_network": net_ms / float(t.min()) - 1.0,
             "regret_analytic": float(t[0, 0] / t.min() - 1.0)}
 
 

@@ -224,9 +224,22 @@ int forward_grid(int n) { return std::max(1, std::min((n + TB - 1) / TB, 4096));
 // ---- installed model
 std::mutex g_model_mu;
 std::vector<float> g_params, g_mean, g_scale;
+std::vector<float> g_lo, g_hi;  // feature range of the training candidates (empty: no limit)
 int g_n_in = 0;
 
 }  // namespace
+
+bool cost_model_in_domain(const float* feats, int n) {
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    if (g_lo.empty()) return true;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < g_n_in; k++) {
+            const float f = feats[(size_t)i * g_n_in + k];
+            const float margin = DOMAIN_MARGIN * (g_hi[k] - g_lo[k]);
+            if (!(f >= g_lo[k] - margin && f <= g_hi[k] + margin)) return false;
+        }
+    return true;
+}
 
 bool cost_model_loaded(int n_in) {
     std::lock_guard<std::mutex> lk(g_model_mu);
@@ -321,7 +334,26 @@ int gbsp_cost_model_set(const float* params, int n_in, const float* feat_mean, c
     gbsp::g_params.assign(params, params + gbsp::layout(n_in).total);
     gbsp::g_mean.assign(feat_mean, feat_mean + n_in);
     gbsp::g_scale.assign(feat_scale, feat_scale + n_in);
+    gbsp::g_lo.clear();  // a new model's domain comes with it
+    gbsp::g_hi.clear();
     gbsp::g_n_in = n_in;
+    return GBSP_OK;
+}
+
+int gbsp_cost_model_set_domain(int n_in, const float* feat_lo, const float* feat_hi) {
+    std::lock_guard<std::mutex> lk(gbsp::g_model_mu);
+    if (!feat_lo && !feat_hi) {
+        gbsp::g_lo.clear();
+        gbsp::g_hi.clear();
+        return GBSP_OK;
+    }
+    if (gbsp::g_params.empty() || n_in != gbsp::g_n_in || !feat_lo || !feat_hi)
+        return set_error(GBSP_ERR_INVALID, "gbsp_cost_model_set_domain: install the model first; n_in must match");
+    for (int k = 0; k < n_in; k++)
+        if (!(feat_lo[k] <= feat_hi[k]))
+            return set_error(GBSP_ERR_INVALID, "gbsp_cost_model_set_domain: feat_lo must be <= feat_hi");
+    gbsp::g_lo.assign(feat_lo, feat_lo + n_in);
+    gbsp::g_hi.assign(feat_hi, feat_hi + n_in);
     return GBSP_OK;
 }
 

@@ -298,7 +298,9 @@ int validate_csc(int rows, int cols, int n_active, int nnz, const int* col_ptr,
 
 // Learned planner: the cost model scores every tuning candidate of the
 // matrix and the cheapest prediction fills in o's radices, row block and
-// pass-1 shape.  The spectrum does not depend on the choice.
+// pass-1 shape.  A matrix whose candidates leave the model's training range
+// (gbsp_cost_model_set_domain) keeps the analytic choice, and o->planner
+// says so.  The spectrum does not depend on the choice.
 int learned_choice(const gbsp_plan_s* p, const int* col_ptr, size_t smem_cap, gbsp_options* o) {
     if (!gbsp::cost_model_loaded(gbsp::N_FEATURES))
         return set_error(GBSP_ERR_INVALID, "planner: no cost model installed (gbsp_cost_model_set)");
@@ -312,6 +314,10 @@ int learned_choice(const gbsp_plan_s* p, const int* col_ptr, size_t smem_cap, gb
         if (int rc = gbsp::plan_features(p->rows, p->cols, p->n_active, p->nnz, col_ptr, &cands[i], smem_cap,
                                          feats.data() + i * gbsp::N_FEATURES))
             return rc;
+    if (!gbsp::cost_model_in_domain(feats.data(), (int)cands.size())) {
+        o->planner = GBSP_PLANNER_MODEL;
+        return GBSP_OK;
+    }
     if (int rc = gbsp::cost_model_predict(feats.data(), (int)cands.size(), pred.data())) return rc;
     const size_t best = std::min_element(pred.begin(), pred.end()) - pred.begin();
     std::memcpy(o->radix, cands[best].radix, sizeof(o->radix));

@@ -70,6 +70,11 @@ int plan_features(int rows, int cols, int n_active, int nnz, const int* col_ptr,
 
 // ---- learned cost model (gbsp_mlp.cu)
 bool cost_model_loaded(int n_in);
+// false when a feature of the n candidates lies outside the installed
+// training range by more than DOMAIN_MARGIN of its width (always true when
+// no range is installed)
+constexpr float DOMAIN_MARGIN = 0.1f;
+bool cost_model_in_domain(const float* feats, int n);
 // Predicted log-latency of n candidates (raw features, n x N_FEATURES).
 int cost_model_predict(const float* feats, int n, float* out);
 

@@ -134,7 +134,8 @@ typedef struct {
     int rows_threads;      /* row-kernel block size in use                                */
     size_t device_bytes;   /* device memory held by the plan                              */
     int pass1_shape;       /* pass-1 shape in use (1-based)                               */
-    int planner;           /* planner that chose the configuration                        */
+    int planner;           /* planner that chose the configuration (GBSP_PLANNER_MODEL
+                              when a learned request fell outside the model's domain)     */
     int channel_mode;      /* 0 single channel, 1 clusters, 2 sequential channels         */
     int exact_phases;      /* 1: every pass-1 twiddle an exact table lookup               */
     int direct;            /* 1: one FFT of length cols per row instead of Bluestein       */
@@ -380,6 +381,12 @@ int gbsp_mlp_adam(float* d_params, const float* d_grad, float* d_m, float* d_v, 
  * inputs are standardised as (x - feat_mean) / feat_scale before the
  * network; the output is log(predicted ms).  n_in must be GBSP_N_FEATURES. */
 int gbsp_cost_model_set(const float* params, int n_in, const float* feat_mean, const float* feat_scale);
+/* Optional, after gbsp_cost_model_set (which clears it): the range of each
+ * feature over the model's training candidates.  A matrix with a candidate
+ * feature outside [lo - m, hi + m], m = 10 % of hi - lo, is planned by the
+ * analytic model instead (its info.planner reads GBSP_PLANNER_MODEL): the
+ * network is not trusted where it never saw data.  NULL, NULL clears it. */
+int gbsp_cost_model_set_domain(int n_in, const float* feat_lo, const float* feat_hi);
 
 #ifdef __cplusplus
 }

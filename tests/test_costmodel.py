@@ -101,6 +101,26 @@ def test_compose_and_regret():
 
 @pytest.mark.skipif(not costmodel.DEFAULT_MODEL.exists() or not costmodel.DEFAULT_DATA.exists(),
                     reason="packaged cost model not trained yet")
+def test_packaged_model_domain():
+    # the stored range is that of the training candidates: every held-out
+    # matrix of the same generator lies inside it, the 40421 x 40421
+    # adjacency (three channels, rows far above 12000) does not
+    ds = costmodel.load_dataset()
+    model = costmodel.load_model()
+    tr, te = costmodel.split(ds)
+    X, _, _ = costmodel.compose(ds, tr)
+    np.testing.assert_array_equal(model["lo"], X.min(0))
+    np.testing.assert_array_equal(model["hi"], X.max(0))
+    for k in te[:50]:
+        Xk, _, _ = costmodel.compose(ds, [k])
+        assert costmodel.in_domain(model, Xk)
+    coo = synthetic.config_matrix("uniform_powerlaw_40421")
+    cands, _, _ = tuning.candidates(coo.rows, coo.cols, length_policy=gb.GBSP_LEN_7SMOOTH, index_bytes=4)
+    assert not costmodel.in_domain(model, np.array([tuning.features(coo, c) for c in cands]))
+
+
+@pytest.mark.skipif(not costmodel.DEFAULT_MODEL.exists() or not costmodel.DEFAULT_DATA.exists(),
+                    reason="packaged cost model not trained yet")
 def test_packaged_model_beats_analytic_planner():
     ds = costmodel.load_dataset()
     model = costmodel.load_model()

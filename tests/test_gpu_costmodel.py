@@ -133,6 +133,35 @@ def test_learned_planner_picks_the_predicted_best(cuda):
     assert fp64.rel_l2(got, ref) < 1e-5
 
 
+def test_learned_planner_outside_its_domain(cuda):
+    # a matrix whose candidates leave the training range (16706 columns: two
+    # channels, which the batch generator never produces) keeps the analytic
+    # choice; clearing the range lets the network decide
+    if not costmodel.DEFAULT_MODEL.exists():
+        pytest.skip("packaged cost model not trained yet")
+    model = costmodel.load_model()
+    assert "lo" in model
+    costmodel.install(model)
+    costmodel._installed = True
+    coo = synthetic.uniform_matrix(2001, 16706, 30000, seed=11)
+    cands, nr, npp = tuning.candidates(coo.rows, coo.cols, length_policy=gb.GBSP_LEN_7SMOOTH)
+    X = np.array([tuning.features(coo, c) for c in cands])
+    assert not costmodel.in_domain(model, X)
+    with gb.Plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, planner="learned") as plan:
+        assert plan.info["planner"] == gb._capi.GBSP_PLANNER_MODEL
+        assert tuple(plan.info["radix"]) == cands[0].radices()
+        assert plan.info["pass1_shape"] == cands[0].pass1_shape
+    lib = gb._capi.load()
+    gb._capi.check(lib.gbsp_cost_model_set_domain(0, None, None), "gbsp_cost_model_set_domain")
+    try:
+        want = cands[int(np.argmin(costmodel.predict(model, X)))]
+        with gb.Plan(coo, length_policy=gb.GBSP_LEN_7SMOOTH, planner="learned") as plan:
+            assert plan.info["planner"] == gb._capi.GBSP_PLANNER_LEARNED
+            assert tuple(plan.info["radix"]) == want.radices()
+    finally:
+        costmodel.install(model)
+
+
 def test_learned_batch(cuda):
     import torch
     if not costmodel.DEFAULT_MODEL.exists():
