@@ -104,12 +104,17 @@ double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta) {
         const double rounds = std::ceil((double)nb / (double)nt);
         // radices 35 and 40 spill at 128 registers a thread: weight 1.5,
         // fitted to the tuner's timings of 2200 matrices (mean row-kernel
-        // regret of the first pick 4.1 % -> 3.7 %)
-        double per = rounds * R * (R > 32 ? 1.5 : 1.0);
+        // regret of the first pick 4.1 % -> 3.7 %).  A fused last stage of
+        // radix 2 or 3 costs twice its share (the filter load and the pairing
+        // are paid per element, with little arithmetic to hide them): 1890
+        // timed matrices 3.4 -> 3.1 %, and on GB300 every x,..,3 plan measured
+        // against its replacement was slower (3460^2 10 %, 40421^2 3-smooth 8 %)
+        const bool last = s == fd.nst - 1;
+        double per = rounds * R * (R > 32 ? 1.5 : 1.0) * (last && R <= 3 ? 2.0 : 1.0);
         const bool strided = (m == 1 && R % 2 == 0) ||
                              (m > 1 && m < 16 && l > 1 && !stage_j_fastest(R, m, l));
         if (strided) per *= 1.5;
-        cost += ((s == fd.nst - 1) ? 1.6 : 2.0) * per + 12.0;
+        cost += (last ? 1.6 : 2.0) * per + 12.0;
     }
     const int regs = nt <= 512 ? 128 : 64;
     int ctas = std::min({(int)(kSmemPerSM / (smem_per_cta + 1024)), 2048 / nt, kRegsPerSM / (nt * regs)});
