@@ -333,31 +333,59 @@ __device__ __forceinline__ void p1_item(const P1Args& a, long it, float2* stage,
         for (int kk = 0; kk < KU; kk++) stage[(lane + 32 * kk) * pitch + col] = acc[kk];
     }
     __syncthreads();
+    // The window leaves through S.  Columns of at most one part: each thread
+    // keeps one column (the block size is a multiple of cw, so every element
+    // it visits has column threadIdx.x % cw) and walks its rows, with the
+    // column's part, chirp and S address in registers; a warp stores 32
+    // consecutive columns of one row.  Columns of several parts (heavy
+    // columns cut for balance) are summed afterwards with one thread per
+    // row, so their compensated sums do not hold up the other lanes.
     const int ncol = min(cw, a.s_cols - c0);
     const int cw_log2 = __ffs(cw) - 1;  // every pass-1 shape's window is 16, 32 or 64 columns
-    for (int e = threadIdx.x; e < UBLK * cw; e += blockDim.x) {
-        const int row = e >> cw_log2, lc = e & (cw - 1);
-        const int ul = ul0 + row;
-        if (ul >= a.tile_rows || lc >= ncol) continue;
-        const int p0 = sh.slot0[lc], p1 = sh.slot0[lc + 1];
-        const float2* srow = stage + row * pitch;
-        float2 v = make_float2(0.f, 0.f);
-        if (p1 - p0 == 1) {
-            v = srow[p0];
-        } else {
-            float2 comp = make_float2(0.f, 0.f);
-            for (int k = p0; k < p1; k++) {  // parts in a fixed order, compensated
-                float y = srow[k].x - comp.x;
-                float t = v.x + y;
-                comp.x = (t - v.x) - y;
-                v.x = t;
-                y = srow[k].y - comp.y;
-                t = v.y + y;
-                comp.y = (t - v.y) - y;
-                v.y = t;
+    const int rend = min(UBLK, a.tile_rows - ul0);
+    const int lc = threadIdx.x & (cw - 1);
+    {
+        const int p0 = sh.slot0[lc], np = sh.slot0[lc + 1] - p0;
+        if (lc < ncol && np <= 1) {
+            const float2 ch = sh.chirp[lc];
+            const int rstep = blockDim.x >> cw_log2;
+            int row = threadIdx.x >> cw_log2;
+            float2* dst = a.S + (size_t)(ul0 + row) * a.s_pitch + c0 + lc;
+            const size_t dstep = (size_t)rstep * a.s_pitch;
+            for (; row < rend; row += rstep, dst += dstep) {
+                const float2 v = np > 0 ? stage[row * pitch + p0] : make_float2(0.f, 0.f);
+                *dst = cmul(v, ch);
             }
         }
-        a.S[(size_t)ul * a.s_pitch + c0 + lc] = cmul(v, sh.chirp[lc]);
+    }
+    // the window's several-part columns, as a bit mask (every warp forms it)
+    uint64_t multi = 0;
+    for (int h = 0; h < cw; h += 32) {
+        const int c = h + (int)(threadIdx.x & 31);
+        const bool m = c < ncol && sh.slot0[c + 1] - sh.slot0[c] > 1;
+        multi |= (uint64_t)__ballot_sync(0xffffffffu, m) << h;
+    }
+    const int n_multi = __popcll(multi);
+    for (int e = threadIdx.x; e < n_multi * UBLK; e += blockDim.x) {
+        const int j = e / UBLK, row = e - j * UBLK;
+        if (row >= rend) continue;
+        uint64_t mm = multi;
+        for (int t = 0; t < j; t++) mm &= mm - 1;  // drop the j lowest set bits
+        const int c = __ffsll((long long)mm) - 1;
+        const int q0 = sh.slot0[c], q1 = sh.slot0[c + 1];
+        const float2* srow = stage + row * pitch;
+        float2 v = srow[q0], comp = make_float2(0.f, 0.f);
+        for (int k = q0 + 1; k < q1; k++) {  // parts in a fixed order, compensated
+            float y = srow[k].x - comp.x;
+            float t = v.x + y;
+            comp.x = (t - v.x) - y;
+            v.x = t;
+            y = srow[k].y - comp.y;
+            t = v.y + y;
+            comp.y = (t - v.y) - y;
+            v.y = t;
+        }
+        a.S[(size_t)(ul0 + row) * a.s_pitch + c0 + c] = cmul(v, sh.chirp[c]);
     }
     if (threadIdx.x == 0) sh.next_task = 0;
     __syncthreads();
