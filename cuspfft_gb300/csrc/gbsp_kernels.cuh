@@ -717,6 +717,50 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
         // rather than once per value.  The channels are summed in order.
         constexpr int WS = 4;
         const float2* zs0 = a.zscratch + (size_t)blockIdx.x * (K - 1) * Lp;
+        if (K == 2) {
+            // Two channels (Lp >= cols, so both read slot c itself): all of
+            // a pass's loads are issued before any product, with no channel
+            // loop and no wrap of c; the sum runs in the general order.
+            const float2* p0 = a.post;
+            const float2* p1 = a.post + cols;
+            for (int s0 = lo + tid; s0 < hi; s0 += WS * nt) {
+                float2 za[WS][2], pa[WS][2], zb[WS][2], pb[WS][2];
+#pragma unroll
+                for (int w = 0; w < WS; w++) {
+                    const int s = s0 + w * nt;
+                    const int sel = s >= half_slots;
+                    const int v = 2 * (s - sel * half_slots);
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const int vv = v + e;
+                        const int c = (s >= hi || vv > hc) ? 0 : sel ? (vv == 0 ? 0 : cols - vv) : vv;
+                        pa[w][e] = __ldg(p0 + c);
+                        za[w][e] = __ldcg(zs0 + c);
+                        pb[w][e] = __ldg(p1 + c);
+                        zb[w][e] = buf[c];
+                    }
+                }
+#pragma unroll
+                for (int w = 0; w < WS; w++) {
+                    const int s = s0 + w * nt;
+                    if (s >= hi) break;
+                    const int sel = s >= half_slots;
+                    const int v = 2 * (s - sel * half_slots);
+                    float2 o[2];
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const float2 y = cadd(cadd(make_float2(0.f, 0.f), cmul(za[w][e], pa[w][e])),
+                                              cmul(zb[w][e], pb[w][e]));
+                        o[e] = (v + e > hc) ? make_float2(0.f, 0.f) : y;
+                        if (sel) o[e].y = -o[e].y;
+                    }
+                    const int row = sel ? u2 : u;
+                    const int drow = row < a.map_split ? row - a.map_lo : row - a.map_hi;
+                    float4* dst = reinterpret_cast<float4*>(a.out + (size_t)drow * a.out_pitch + v);
+                    __stcs(dst, make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
+                }
+            }
+        } else
         for (int s0 = lo + tid; s0 < hi; s0 += WS * nt) {
             int cc[WS][2], nn[WS][2];
             float2 acc[WS][2];
