@@ -389,6 +389,36 @@ __device__ __forceinline__ void fft_stage(V* __restrict__ buf, int Lp, int m, ui
     }
 }
 
+// The first forward stage reading its inputs straight from global memory
+// (the sequential-channel rows: no bulk copy into shared memory, no separate
+// pre-twiddle pass): x[n] = src[n] * pre[n] (PRE) or src[n] for n < cols,
+// zero beyond.  Stage 0 has span m = Lp / R and one block, so butterfly k
+// reads x[k + s*m]; results go to buf in the stage's usual places.
+template <int R, bool PRE, typename V>
+__device__ __forceinline__ void fft_stage0_global(V* __restrict__ buf, const V* __restrict__ src,
+                                                  const V* __restrict__ pre, int cols, int m,
+                                                  const V* __restrict__ tw, int tid, int nthreads) {
+    using RX = Radix<R>;
+    for (int k = tid; k < m; k += nthreads) {
+        V a[R];
+#pragma unroll
+        for (int s = 0; s < R; s++) {
+            const int idx = k + s * m;
+            V x = mk<V>(0.f, 0.f);
+            if (idx < cols) {
+                x = __ldcg(src + idx);
+                if (PRE) x = cmul(x, __ldg(pre + idx));
+            }
+            a[s] = x;
+        }
+        RX::fwd(a);
+#pragma unroll
+        for (int q = 1; q < R; q++) a[RX::out_reg(q)] = cmul(a[RX::out_reg(q)], __ldg(tw + k + (q - 1) * m));
+#pragma unroll
+        for (int q = 0; q < R; q++) buf[k + q * m] = a[RX::out_reg(q)];
+    }
+}
+
 // Radices the row kernel supports; the plan only emits these.  A kernel
 // compiled for blocks of up to 1024 threads (64 registers a thread) holds
 // radices up to 16; the 512-thread variant (128 registers) all of them.
@@ -418,6 +448,23 @@ __device__ __forceinline__ bool fft_stage_dispatch(int R, V* buf, int Lp, int m,
             return false;
         GBSP_RADIX_LIST(GBSP_STAGE_CASE)
 #undef GBSP_STAGE_CASE
+        default: return false;
+    }
+}
+
+template <int MAXR, bool PRE, typename V>
+__device__ __forceinline__ bool fft_stage0_global_dispatch(int R, V* buf, const V* src, const V* pre, int cols,
+                                                           int m, const V* tw, int tid, int nthreads) {
+    switch (R) {
+#define GBSP_STAGE0_CASE(r)                                                                  \
+        case r:                                                                              \
+            if constexpr (r <= MAXR) {                                                       \
+                fft_stage0_global<r, PRE>(buf, src, pre, cols, m, tw, tid, nthreads);        \
+                return true;                                                                 \
+            }                                                                                \
+            return false;
+        GBSP_RADIX_LIST(GBSP_STAGE0_CASE)
+#undef GBSP_STAGE0_CASE
         default: return false;
     }
 }

@@ -563,8 +563,14 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
     for (int qc = SEQ ? 0 : q; qc < q_end; qc++) {
         const float2* preq = a.pre + (size_t)qc * cols;
         const float2* filtq = a.filt + (size_t)qc * Lp;
+        // Sequential channels whose row fits the channel (no fold) and whose
+        // network has a separate first stage read the row straight from
+        // global memory in that stage, pre-twiddle included
+        const int S1 = fd.nst - 1;
+        const bool g0 = SEQ && cols_even <= Lp && S1 > 0;
         // (a single channel always has cols_even <= Lp: L >= 2*cols - 1)
-        if (!MULTI || cols_even <= Lp) {
+        if (g0) {
+        } else if (!MULTI || cols_even <= Lp) {
             if (tid == 0) {
                 fence_proxy_async_smem();
                 mbar_expect_tx(bar, (uint32_t)cols_even * 8u);
@@ -621,12 +627,17 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
             __syncthreads();
         }
         // forward DIF, filter multiply fused with the last stage, inverse DIT
-        const int S1 = fd.nst - 1;
         const float2* none = nullptr;
         // (a direct plan runs the forward network alone, its last stage --
         // span 1, twiddles exactly 1 -- included: X in digit-reversed order)
         const int S_fwd = direct ? S1 + 1 : S1;
-        if (S_fwd > 0) {
+        if (SEQ && g0) {
+            ok &= (qc == 0) ? fft_stage0_global_dispatch<MAXR, false>(fd.R[0], buf, srow, none, cols, fd.m[0], tw0,
+                                                                       tid, nt)
+                            : fft_stage0_global_dispatch<MAXR, true>(fd.R[0], buf, srow, preq, cols, fd.m[0], tw0,
+                                                                      tid, nt);
+            __syncthreads();
+        } else if (S_fwd > 0) {
             ok &= fft_stage_dispatch<0, MAXR, true>(fd.R[0], buf, Lp, fd.m[0], fd.magic[0], tw0, none, tid, nt);
             __syncthreads();
         }
