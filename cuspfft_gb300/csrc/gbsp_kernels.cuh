@@ -567,7 +567,7 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
         // network has a separate first stage read the row straight from
         // global memory in that stage, pre-twiddle included
         const int S1 = fd.nst - 1;
-        const bool g0 = SEQ && cols_even <= Lp && S1 > 0;
+        const bool g0 = (SEQ || CLUSTER) && cols_even <= Lp && S1 > 0;
         // (a single channel always has cols_even <= Lp: L >= 2*cols - 1)
         if (g0) {
         } else if (!MULTI || cols_even <= Lp) {
@@ -631,7 +631,7 @@ __device__ __forceinline__ void bluestein_row(const RowsArgs& a, const FFTDesc& 
         // (a direct plan runs the forward network alone, its last stage --
         // span 1, twiddles exactly 1 -- included: X in digit-reversed order)
         const int S_fwd = direct ? S1 + 1 : S1;
-        if (SEQ && g0) {
+        if ((SEQ || CLUSTER) && g0) {
             ok &= (qc == 0) ? fft_stage0_global_dispatch<MAXR, false>(fd.R[0], buf, srow, none, cols, fd.m[0], tw0,
                                                                        tid, nt)
                             : fft_stage0_global_dispatch<MAXR, true>(fd.R[0], buf, srow, preq, cols, fd.m[0], tw0,
