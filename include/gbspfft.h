@@ -189,10 +189,11 @@ int gbsp_plan_get_info(gbsp_plan_t plan, gbsp_plan_info* info);
 int gbsp_plan_destroy(gbsp_plan_t plan);
 
 /* Freed plan memory the library's pool keeps for later plans, per device
- * (default 1 GiB): a cudaMalloc and a cudaFree of a plan's allocation cost
- * ~0.1 ms each, a pooled one a few microseconds.  Memory above the limit
- * goes back to the CUDA driver at the next synchronisation; 0 keeps nothing.
- * Takes effect at once (trims the pools to the new limit). */
+ * (default 1 GiB), on top of the memory of the plans alive: a cudaMalloc and
+ * a cudaFree of a plan's allocation cost ~0.1 ms each, a pooled one a few
+ * microseconds.  Free memory above the limit goes back to the CUDA driver
+ * at the next synchronisation; 0 keeps nothing.  Takes effect at once (trims
+ * the pools to the live plans plus the new limit). */
 int gbsp_set_memory_cache(size_t bytes);
 
 /* Runs the transform: the reference's timed tile loop
