@@ -507,7 +507,8 @@ def main():
         e2e = {"value": round(statistics.median(times), 4), "unit": "ms/FFT", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": int(out_bytes), "steps": len(times),
                "includes": "plan build from host CSC (upload, FP64 tables, 1024-row scratch and streaming slabs), "
-                           "transform streamed in automatic tiles (about rows/18, a multiple of the SM count) to "
+                           "transform streamed in automatic tiles (about rows/18, a multiple of the SM count, "
+                           "after a ramp from 256 rows) to "
                            "pinned host memory with the D2H copies overlapping compute (gbsp_execute_to_host), "
                            "plan release"}
 
