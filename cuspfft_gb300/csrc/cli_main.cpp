@@ -6,7 +6,7 @@
 //                 [--csc-mixed-radix-graph] [--csc-tile N] [--repeat N]
 //                 [--sparse-only] [--dense-only] [--cpu-reference] ...
 //
-// Methods the reference offers but this build does not implement print the
+// Methods the reference offers but this library does not implement print the
 // reference's failure row ("<label>  OOM  OOM  [reason]").
 #include <cuda_runtime.h>
 
@@ -112,7 +112,7 @@ void usage(const char* prog) {
             "  --cpu-reference  Host FP64 reference spectrum; every method is checked against it\n"
             "  --repeat N       1 warm-up + N timed runs; report median, min, max (default 1)\n"
             "  (--csc-bluestein --csc-stockham --csc-stockham-graph, which select nothing in the\n"
-            "   reference CLI, and --spfft are accepted and report 'not in this build')\n",
+            "   reference CLI, and --spfft are accepted and report 'not in this library')\n",
             prog);
 }
 
@@ -181,7 +181,7 @@ int main(int argc, char** argv) {
                 printf("%-26s  %10s  %12s  [%s]\n", "CPU reference (FP64)", "FAIL", "FAIL", e.what());
             }
         }
-        if (run_dense) print_fail("Dense cuFFT (baseline)", "not in this build");
+        if (run_dense) print_fail("Dense cuFFT (baseline)", "not in this library");
 
         struct M { bool on; const char* label; const char* check; std::function<SparseFFTResult()> fn; };
         // rows in the reference CLI's order (src/main.cu:480-700)
@@ -219,7 +219,7 @@ int main(int argc, char** argv) {
             }
         }
         if (run_sparse)
-            for (auto& f : unbuilt) print_fail(f.c_str(), "not in this build");
+            for (auto& f : unbuilt) print_fail(f.c_str(), "not in this library");
         printf("\n");
     } catch (const std::exception& e) {
         fprintf(stderr, "Fatal error: %s\n", e.what());

@@ -58,7 +58,7 @@ const char* gbsp_status_string(int status) {
         case GBSP_ERR_ALLOC: return "allocation failed";
         case GBSP_ERR_UNSUPPORTED: return "unsupported shape";
         case GBSP_ERR_IO: return "I/O or parse error";
-        case GBSP_ERR_NOT_BUILT: return "not in this build";
+        case GBSP_ERR_NOT_BUILT: return "not in this library";
         default: return "unknown status";
     }
 }

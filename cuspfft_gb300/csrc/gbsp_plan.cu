@@ -165,6 +165,17 @@ int helper_stream(int dev, cudaStream_t* hs) {
     return GBSP_OK;
 }
 
+// the streaming path's copy stream and events, created once per plan
+int stream_objects(gbsp_plan_s* p) {
+    if (p->stream_cs) return GBSP_OK;
+    GB_CUDA(cudaStreamCreateWithFlags(&p->stream_cs, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; b++) {
+        GB_CUDA(cudaEventCreateWithFlags(&p->stream_done[b], cudaEventDisableTiming));
+        GB_CUDA(cudaEventCreateWithFlags(&p->stream_copied[b], cudaEventDisableTiming));
+    }
+    return GBSP_OK;
+}
+
 void free_plan(gbsp_plan_s* p) {
     if (!p) return;
     if (p->arena && p->arena_pooled) {
@@ -503,6 +514,9 @@ int plan_build(gbsp_plan_s* p, const int* col_ptr, const int* row_idx, const int
         for (int b = 0; b < 2; b++)
             if ((rc = dev_alloc(p, &p->stream_slab[b], stream_slab))) return rc;
         p->stream_slab_bytes = stream_slab;
+        // the copy stream and its events too, so a streamed transform does
+        // no setup of its own
+        if ((rc = stream_objects(p))) return rc;
     }
     if ((p->row_mode == gbsp::ROW_SEQ || p->row_mode == gbsp::ROW_SEQW) &&
         (rc = dev_alloc(p, (void**)&p->d_zscratch, (size_t)p->rows_grid * (K - 1) * Lp * sizeof(float2))))
@@ -1225,13 +1239,7 @@ extern "C" int gbsp_execute_to_host(gbsp_plan_t p, void* h_out, size_t out_pitch
     const int tile = std::min(tile_rows > 0 ? tile_rows : p->stream_tile_auto, p->u_tile);
     cudaStream_t st = (cudaStream_t)stream;
     const size_t slab_bytes = (size_t)2 * tile * out_pitch * sizeof(float2);
-    if (!p->stream_cs) {
-        GB_CUDA(cudaStreamCreateWithFlags(&p->stream_cs, cudaStreamNonBlocking));
-        for (int b = 0; b < 2; b++) {
-            GB_CUDA(cudaEventCreateWithFlags(&p->stream_done[b], cudaEventDisableTiming));
-            GB_CUDA(cudaEventCreateWithFlags(&p->stream_copied[b], cudaEventDisableTiming));
-        }
-    }
+    if (int rc0 = stream_objects(p)) return rc0;
     if (p->stream_slab_bytes < slab_bytes) {
         for (int b = 0; b < 2; b++) {
             if (p->stream_slab[b] && p->stream_slab_owned) {

@@ -3,7 +3,7 @@
 //
 // The reference fills this role with a single-threaded FFTW3f
 // fftwf_plan_dft_r2c_2d (src/cpu_reference.cpp:8-63); FFTW is a third-party
-// library this build does not link, so the CLI evaluates the transform
+// library this project does not link, so the CLI evaluates the transform
 // directly in double precision: exact integer phases (u*r mod rows) along the
 // rows, then a Bluestein FP64 FFT (radix-2 core) along the columns.
 #pragma once

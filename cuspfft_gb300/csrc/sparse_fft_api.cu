@@ -88,12 +88,16 @@ void check_device_flags(gbsp_plan_t p, const char* who) {
     check(gbsp_device_flags_status(flags), who);
 }
 
-void make_plan(const COOMatrix& coo, int u_tile, int policy, PlanHolder& ph, gbsp_plan_info& info) {
+// stream_tile > 0 reserves the streaming slabs (and copy stream) with the
+// plan, outside the timed transform
+void make_plan(const COOMatrix& coo, int u_tile, int policy, PlanHolder& ph, gbsp_plan_info& info,
+               int stream_tile = 0) {
     if (u_tile <= 0) throw std::runtime_error("CSC tile size must be positive");
     CompactCSC csc = make_compact_csc(coo);
     gbsp_options o = {};
     o.length_policy = policy;
     o.u_tile = u_tile;
+    o.stream_tile_rows = stream_tile;
     check(gbsp_plan_create(coo.rows, coo.cols, csc.n_sparse_cols, coo.nnz, csc.col_ptr.data(),
                            csc.row_idx.data(), csc.sparse_cols.data(), &o, nullptr, &ph.p),
           "gbsp_plan_create");
@@ -170,7 +174,7 @@ struct PinnedBuf {
 SparseFFTResult run_streaming(const COOMatrix& coo, int u_tile, int policy) {
     PlanHolder ph;
     gbsp_plan_info info;
-    make_plan(coo, u_tile, policy, ph, info);
+    make_plan(coo, u_tile, policy, ph, info, u_tile);
     const size_t n = (size_t)coo.rows * info.output_pitch;
     PinnedBuf host;
     cuda_check(cudaMallocHost(&host.p, std::max<size_t>(n, 1) * sizeof(cuFloatComplex)), "cudaMallocHost");

@@ -30,7 +30,7 @@ enum {
     GBSP_ERR_INVALID = 1,     /* bad argument (sizes, pointers, options)      */
     GBSP_ERR_CUDA = 2,        /* a CUDA runtime call or kernel launch failed  */
     GBSP_ERR_ALLOC = 3,       /* device or host allocation failed             */
-    GBSP_ERR_UNSUPPORTED = 4, /* shape outside what this build handles        */
+    GBSP_ERR_UNSUPPORTED = 4, /* shape outside what this library handles      */
     GBSP_ERR_IO = 5,          /* file could not be opened / parsed            */
     GBSP_ERR_NOT_BUILT = 6    /* entry point exists for link compatibility only */
 };

@@ -16,14 +16,13 @@ def test_golden_log_parses():
     rows = parse_log(GOLDEN.read_text())
     by = {r["method"]: r for r in rows}
     for label in ("Sparse CSC (mixed-radix)", "Sparse CSC (cufft smooth)", "Sparse CSC (mr-graph)",
-                  "Sparse CSC (cufft stream)", "Sparse CSC (Stockham strm)"):
+                  "Sparse CSC (cufft stream)", "Sparse CSC (Stockham strm)", "Sparse CSC (binary LUT)"):
         r = by[label]
         assert float(r["median_ms"]) > 0 and r["n_iters"] == "3"
         assert float(r["min_ms"]) <= float(r["median_ms"]) <= float(r["max_ms"])
         assert float(r["max_rel"]) < 1e-4, r
     assert by["CPU reference (FP64)"]["n_iters"] == "1"
-    assert by["Dense cuFFT (baseline)"]["error"] == "not in this build"
-    assert by["--csc-binary-lut"]["error"] == "not in this build"
+    assert by["Dense cuFFT (baseline)"]["error"] == "not in this library"
     assert rows[0]["rows"] == "301" and rows[0]["cols"] == "250"
 
 
