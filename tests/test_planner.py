@@ -69,3 +69,26 @@ def test_single_channel_when_the_row_fits(rows, cols):
         assert all(int(np.prod(c.radices())) == row_fft_length(cols, policy) for c in cands)
         forced, _, _ = tuning.candidates(rows, cols, length_policy=policy, force_bluestein=1)
         assert all(int(np.prod(c.radices())) == bluestein_length(cols, policy) for c in forced)
+
+
+@pytest.mark.parametrize("cols,policy,length,channels", [
+    (12100, gb.GBSP_LEN_7SMOOTH, 24300, 1),    # a Bluestein length above 24000 still fits one CTA
+    (13000, gb.GBSP_LEN_7SMOOTH, 26244, 1),
+    (25000, gb.GBSP_LEN_7SMOOTH, 25000, 1),    # smooth columns: one direct FFT of length cols
+    (16706, gb.GBSP_LEN_7SMOOTH, 33600, 2),    # 33600 points do not fit: two channels
+    (40421, gb.GBSP_LEN_7SMOOTH, 81000, 3),
+    (40421, gb.GBSP_LEN_3SMOOTH, 82944, 3),
+])
+def test_smallest_channel_count_that_fits(cols, policy, length, channels):
+    # the convolution splits into the fewest channels whose buffer and inner
+    # twiddles fit in shared memory (measured fastest in 15 of 18 cases)
+    cands, _, _ = tuning.candidates(4001, cols, length_policy=policy)
+    lp = {int(np.prod(c.radices())) for c in cands}
+    assert lp == {length // channels}, lp
+
+
+def test_channel_length_cap_still_applies():
+    # max_channel_len bounds the channel: 40421 columns at 24000 points run
+    # as five channels of 16200
+    cands, _, _ = tuning.candidates(4001, 40421, length_policy=gb.GBSP_LEN_7SMOOTH, max_channel_len=24000)
+    assert {int(np.prod(c.radices())) for c in cands} == {16200}
