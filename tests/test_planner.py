@@ -92,3 +92,13 @@ def test_channel_length_cap_still_applies():
     # as five channels of 16200
     cands, _, _ = tuning.candidates(4001, 40421, length_policy=gb.GBSP_LEN_7SMOOTH, max_channel_len=24000)
     assert {int(np.prod(c.radices())) for c in cands} == {16200}
+
+
+@pytest.mark.parametrize("cols,policy", [(40421, gb.GBSP_LEN_3SMOOTH), (3460, gb.GBSP_LEN_3SMOOTH),
+                                         (9861, gb.GBSP_LEN_7SMOOTH), (5088, gb.GBSP_LEN_7SMOOTH)])
+def test_first_pick_avoids_a_radix_3_fused_stage(cols, policy):
+    # a last (fused) stage of radix 2 or 3 costs twice its share in the row
+    # model: these lengths used to rank an x, ..., 3 plan first, measured
+    # 4-10 % slower on GB300 than the plan ranked first now
+    cands, _, npp = tuning.candidates(4001, cols, length_policy=policy)
+    assert cands[0].radices()[-1] > 3, cands[0].radices()
