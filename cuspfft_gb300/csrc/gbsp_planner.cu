@@ -97,7 +97,7 @@ int max_radix_for(int nt_max) { return nt_max > 512 ? MAX_RADIX_NT1024 : MAX_RAD
 constexpr size_t kSmemPerSM = 233472;
 constexpr int kRegsPerSM = 65536;
 
-double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta) {
+double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta, bool direct) {
     double cost = 0.0;
     for (int s = 0; s < fd.nst; s++) {
         const int R = fd.R[s], m = fd.m[s], nb = fd.Lp / R, l = nb / m;
@@ -113,7 +113,16 @@ double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta) {
         double per = rounds * R * (R > 32 ? 1.5 : 1.0) * (last && R <= 3 ? 2.0 : 1.0);
         const bool strided = (m == 1 && R % 2 == 0) ||
                              (m > 1 && m < 16 && l > 1 && !stage_j_fastest(R, m, l));
-        if (strided) per *= 1.5;
+        if (direct && m == 1 && R % 2 == 0) {
+            // A span-1 stage of even radix reads buf[t*R + s]: its bank
+            // conflicts grow with R's power-of-two part.  Fitted on direct
+            // plans only (GB300, 4001 rows, eight candidates each at seven
+            // smooth lengths): the first pick's mean regret 11.1 -> 3.5 %
+            // (cols 4096: [16, 16, 16] 0.121 ms -> [16, 8, 8, 4] 0.094 ms).
+            per *= std::max(1.5, (double)(R & -R) / 4.0);
+        } else if (strided) {
+            per *= 1.5;
+        }
         cost += (last ? 1.6 : 2.0) * per + 12.0;
     }
     const int regs = nt <= 512 ? 128 : 64;
@@ -122,7 +131,7 @@ double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta) {
     return cost / ctas;
 }
 
-std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt) {
+std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt, bool direct) {
     std::vector<std::vector<int>> cands;
     if (radix_opt && radix_opt[0] > 0) {
         std::vector<int> rs;
@@ -148,7 +157,7 @@ std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_op
             RadixPlan rp;
             rp.fd = fd;
             rp.nt = nt;
-            rp.cost = rows_cost(fd, nt, rows_smem_bytes(fd));
+            rp.cost = rows_cost(fd, nt, rows_smem_bytes(fd), direct);
             out.push_back(rp);
         }
     }
@@ -177,7 +186,7 @@ int split_channels(int cols, const gbsp_options* o, size_t smem_cap, ChannelSpli
     // Bluestein convolution, with a quarter of its FFT work and less rounding
     out->direct = 0;
     if (!(o && o->force_bluestein) && channel_fits(cols) && next_smooth(cols, policy) == cols) {
-        auto ranked = rank_radices(cols, smem_cap, o ? o->radix : nullptr, nt_opt);
+        auto ranked = rank_radices(cols, smem_cap, o ? o->radix : nullptr, nt_opt, true);
         if (!ranked.empty()) {
             out->L = cols;
             out->K = 1;
@@ -381,7 +390,9 @@ int plan_features(int rows, int cols, int n_active, int nnz, const int* col_ptr,
     const int regs = rp.nt <= 512 ? 128 : 64;
     f[26] = (float)std::max(1, std::min({(int)(233472 / (rows_smem_bytes(fd) + 1024)), 2048 / rp.nt,
                                          65536 / (rp.nt * regs)}));
-    f[27] = lg2(rp.cost);
+    // (the Bluestein form of the row model for every plan: the feature the
+    // cost model was trained on)
+    f[27] = lg2(rows_cost(fd, rp.nt, rows_smem_bytes(fd)));
     // pass-1 shape (the two-level shapes share the slot of their half-table
     // twin: the model never saw them, and they only appear when nothing else fits)
     f[28 + (sh_idx == 6 ? 1 : sh_idx == 7 ? 5 : sh_idx)] = 1.f;

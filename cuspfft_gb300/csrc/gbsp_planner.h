@@ -15,7 +15,8 @@ int build_fft_desc(int Lp, const std::vector<int>& rs, FFTDesc* fd);
 int fft_tw_count(const FFTDesc& fd);
 size_t rows_smem_bytes(const FFTDesc& fd);
 int max_radix_for(int nt_max);  // largest radix a block of at most nt_max threads holds
-double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta);
+// direct: the plan is one forward FFT (no Bluestein convolution)
+double rows_cost(const FFTDesc& fd, int nt, size_t smem_per_cta, bool direct = false);
 
 struct RadixPlan {
     FFTDesc fd{};
@@ -25,7 +26,8 @@ struct RadixPlan {
 // Every (radix sequence, block size) for channel length Lp that fits in
 // smem_cap, cheapest first by rows_cost.  radix_opt (0-terminated, may be
 // null) and nt_opt (0 = automatic: 256 or 512) restrict the set.
-std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt);
+std::vector<RadixPlan> rank_radices(int Lp, size_t smem_cap, const int* radix_opt, int nt_opt,
+                                    bool direct = false);
 
 // Channel split of the length-L convolution: the smallest K (<= MAX_CHANNELS
 // for clusters, MAX_SEQ_CHANNELS for sequential channels)
