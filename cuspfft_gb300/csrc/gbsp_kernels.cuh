@@ -482,8 +482,11 @@ k_twiddle_sum_batch(const P1Args* __restrict__ args, const long* __restrict__ it
 // (u <= rows/2) writes output rows u and rows-u, each with 16-byte stores of
 // two complex values.
 //
-// The input row arrives with one bulk copy (cp.async.bulk) straight into the
-// FFT buffer whenever it fits (columns rounded up to even <= Lp); otherwise
+// A single-channel row arrives with one bulk copy (cp.async.bulk) straight
+// into the FFT buffer.  A channel of a multi-channel row whose columns fit
+// the channel (columns rounded up to even <= Lp) is read from global memory
+// by its first forward stage, pre-twiddle included (no copy, zero fill or
+// pre-twiddle pass; with a one-stage network, by the bulk copy); otherwise
 // (several columns folding onto one slot) it is added section by section.
 //
 // Shared memory: the row buffer, then the twiddles of stages >= 1 (loaded
